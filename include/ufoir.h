@@ -1,0 +1,292 @@
+/*
+ * ufoir.h - C ABI of the GB300-native ufo-ir iterative-reconstruction path.
+ *
+ * The library (libufoir.so) replaces ufo-ir's OpenCL hot path: the
+ * parallel-beam Joseph projector plugin and the SART / SIRT / ASD-POCS /
+ * split-Bregman-TV method plugins built on it. Kernels are hand-written CUDA
+ * for sm_103a; the host side is C. No OpenCL, no CPU fallback: every compute
+ * entry point runs on the GPU or fails with a status code.
+ *
+ * Each entry point names the reference interface it replaces as
+ * file:line within the ufo-ir source tree.
+ *
+ * Conventions
+ *   - Every call returns 0 (UFOIR_OK) or a negative ufoir_status; the last
+ *     error message of a context is available through ufoir_last_error().
+ *     Nothing aborts the process and no device code traps.
+ *   - Data are float32, row-major with x fastest, exactly as a UfoBuffer's
+ *     host array: a sinogram is [n_angles][n_dets], a volume (the
+ *     reconstruction grid) is [n_dets][n_dets] (the reference always
+ *     reconstructs an n_dets x n_dets grid,
+ *     src/tasks/ufo-ir-parallel-projector-task.c:339-346, :576-578).
+ *     n_slices > 1 means that many independent slices stored back to back.
+ *   - Data pointers may be host memory (pageable or pinned) or device memory
+ *     of the context's GPU; the library detects which and stages host data
+ *     through HBM itself. Device pointers keep the data resident.
+ *   - Calls on one context are serialised on that context's CUDA stream and
+ *     return after the result is complete (ufo-core's process() is synchronous).
+ */
+#ifndef UFOIR_H
+#define UFOIR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define UFOIR_API __attribute__((visibility("default")))
+#else
+#define UFOIR_API
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes. The reference logs OpenCL errors and continues, and aborts */
+/* on shape errors through g_error (src/core/ufo-ir-basic-ops.c:48, :222);  */
+/* this ABI returns a status instead.                                        */
+/* ------------------------------------------------------------------------ */
+typedef enum {
+    UFOIR_OK = 0,
+    UFOIR_ERR_INVALID = -1,      /* bad argument, shape or parameter range */
+    UFOIR_ERR_CUDA = -2,         /* CUDA runtime error (message has details) */
+    UFOIR_ERR_NOMEM = -3,        /* device or host allocation failed */
+    UFOIR_ERR_UNSUPPORTED = -4,  /* e.g. a projector model other than "joseph" */
+    UFOIR_ERR_BUDGET = -5,       /* request larger than the HBM budget */
+    UFOIR_ERR_TIMEOUT = -6,      /* a bounded wait ran out */
+    UFOIR_ERR_CANCELLED = -7,    /* job cancelled */
+    UFOIR_ERR_STATE = -8,        /* object used in the wrong state */
+    UFOIR_ERR_NOT_FOUND = -9     /* unknown job id */
+} ufoir_status;
+
+/* ------------------------------------------------------------------------ */
+/* Context: one GPU, one stream, a device memory pool. Replaces ufo-core's  */
+/* UfoResources + UfoGpuNode command queue that the plugins borrow          */
+/* (src/core/ufo-ir-method-task.c:235-238 declares UFO_TASK_MODE_GPU;      */
+/* src/tasks/ufo-ir-sart-task.c:162 hands the node to the projector).       */
+/* ------------------------------------------------------------------------ */
+typedef struct ufoir_ctx ufoir_ctx;
+
+/* Create a context on CUDA device `device`. hbm_budget_bytes caps what the
+ * serve loop admits (0 = 90% of free memory at creation). */
+UFOIR_API int ufoir_ctx_create(int device, uint64_t hbm_budget_bytes, ufoir_ctx **out);
+UFOIR_API void ufoir_ctx_destroy(ufoir_ctx *ctx);
+/* Message of the last failed call on this context ("" if none). */
+UFOIR_API const char *ufoir_last_error(const ufoir_ctx *ctx);
+UFOIR_API int ufoir_ctx_synchronize(ufoir_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+UFOIR_API void *ufoir_ctx_stream(ufoir_ctx *ctx);
+/* Device memory helpers (stream-ordered on the context's stream). */
+UFOIR_API int ufoir_device_alloc(ufoir_ctx *ctx, size_t bytes, void **ptr);
+UFOIR_API int ufoir_device_free(ufoir_ctx *ctx, void *ptr);
+/* Page-locked host memory (for fast staging of host inputs/outputs). */
+UFOIR_API int ufoir_host_alloc(ufoir_ctx *ctx, size_t bytes, void **ptr);
+UFOIR_API int ufoir_host_free(ufoir_ctx *ctx, void *ptr);
+/* Copy between any combination of host and device memory; synchronous. */
+UFOIR_API int ufoir_memcpy(ufoir_ctx *ctx, void *dst, const void *src, size_t bytes);
+/* Number of kernels this library launched on the context so far. */
+UFOIR_API uint64_t ufoir_ctx_kernel_launches(const ufoir_ctx *ctx);
+/* CUDA-event timer on the context's stream: begin records a start event,
+ * end records a stop event, waits for it and returns the elapsed device time. */
+UFOIR_API int ufoir_ctx_timer_begin(ufoir_ctx *ctx);
+UFOIR_API int ufoir_ctx_timer_end(ufoir_ctx *ctx, float *ms);
+
+/* ------------------------------------------------------------------------ */
+/* Projector: the "parallel-projector" plugin (package "ir").                */
+/* ------------------------------------------------------------------------ */
+
+/* Direction of a run of angles; same values as UfoIrProjectionDirection
+ * (src/tasks/ufo-ir-parallel-projector-task.h:37-40). */
+enum { UFOIR_HORIZONTAL = 0, UFOIR_VERTICAL = 1 };
+
+/* UfoIrProjectionsSubset (…parallel-projector-task.h:49-53). */
+typedef struct {
+    unsigned int offset;   /* first angle */
+    unsigned int n;        /* number of angles */
+    int direction;         /* UFOIR_HORIZONTAL (|sin| > |cos|) or UFOIR_VERTICAL */
+} ufoir_subset;
+
+/* Properties of the projector node, with the reference's names, ranges and
+ * defaults (JSON keys in brackets):
+ *   model            ["model"]            "joseph"      (…parallel-projector-task.c:123-128)
+ *   angles_num       ["angles_num"]       0 = from input dims[1] (:132-137, :315-317)
+ *   is_forward       ["is_forward"]       1             (src/core/ufo-ir-state-dependent-task.c:75-80)
+ *   axis_position    ["axis_position"]    -1 = n_dets/2 (src/core/ufo-ir-projector-task.c:68-73)
+ *   step             ["step"]             0 rad         (:75-80)
+ *   relaxation       ["relaxation"]       1             (:82-87)
+ *   correction_scale ["correction_scale"] 1             (:88-93) */
+typedef struct {
+    char model[32];
+    unsigned int angles_num;
+    int is_forward;
+    float axis_position;
+    float step;
+    float relaxation;
+    float correction_scale;
+} ufoir_projector_params;
+
+typedef struct ufoir_projector ufoir_projector;
+
+UFOIR_API void ufoir_projector_params_init(ufoir_projector_params *p);
+/* ufo_ir_parallel_projector_task_new (…parallel-projector-task.c:79-82) + setup (:360-388).
+ * Fails with UFOIR_ERR_UNSUPPORTED unless model is "joseph" (case-insensitive,
+ * the reference lower-cases it, :283-287). */
+UFOIR_API int ufoir_projector_create(ufoir_ctx *ctx, const ufoir_projector_params *p,
+                                     ufoir_projector **out);
+UFOIR_API void ufoir_projector_destroy(ufoir_projector *proj);
+/* GObject get/set of the properties above (…projector-task.c:212-259,
+ * src/core/ufo-ir-projector-task.c:113-164). */
+UFOIR_API int ufoir_projector_get_params(const ufoir_projector *proj, ufoir_projector_params *p);
+UFOIR_API int ufoir_projector_set_params(ufoir_projector *proj, const ufoir_projector_params *p);
+
+/* get_requisition (…parallel-projector-task.c:306-347): in_dims = {dims[0],
+ * dims[1]} of the input buffer; (re)builds the sin/cos LUT and the direction
+ * subsets when the angle count changes; out_dims = {n_dets, n_angles} when
+ * is_forward, {n_dets, n_dets} otherwise. */
+UFOIR_API int ufoir_projector_get_requisition(ufoir_projector *proj, const size_t in_dims[2],
+                                              size_t out_dims[2]);
+/* UfoTask process of the standalone node (src/core/ufo-ir-state-dependent-task.c:195-212):
+ * zero the output, then forward (is_forward) or backward projection. */
+UFOIR_API int ufoir_projector_process(ufoir_projector *proj, const float *in,
+                                      const size_t in_dims[2], float *out, size_t n_slices);
+/* Vtable forward/backward over the full direction subsets, accumulating
+ * into the output (…parallel-projector-task.c:391-429):
+ *   sino += correction_scale * A vol ;   vol += relaxation * A^T sino. */
+UFOIR_API int ufoir_projector_forward(ufoir_projector *proj, const float *vol, float *sino,
+                                      size_t n_dets, size_t n_angles, size_t n_slices);
+UFOIR_API int ufoir_projector_backward(ufoir_projector *proj, float *vol, const float *sino,
+                                       size_t n_dets, size_t n_angles, size_t n_slices);
+/* ufo_ir_parallel_projector_subset_fp / _subset_bp (…parallel-projector-task.h:93-94,
+ * .c:167-195): one subset, accumulating; the geometry must have been set by
+ * a requisition or a forward/backward call. */
+UFOIR_API int ufoir_projector_subset_fp(ufoir_projector *proj, const float *vol, float *sino,
+                                        const ufoir_subset *subset);
+UFOIR_API int ufoir_projector_subset_bp(ufoir_projector *proj, float *vol, const float *sino,
+                                        const ufoir_subset *subset);
+/* get_host_sin_vals / get_host_cos_vals (…parallel-projector-task.h:96-97);
+ * NULL before the first requisition. */
+UFOIR_API const float *ufoir_projector_get_host_sin_vals(const ufoir_projector *proj);
+UFOIR_API const float *ufoir_projector_get_host_cos_vals(const ufoir_projector *proj);
+/* The full direction-subset list (…parallel-projector-task.c:462-498). */
+UFOIR_API int ufoir_projector_get_subsets(const ufoir_projector *proj, const ufoir_subset **subsets,
+                                          unsigned int *count);
+
+/* ------------------------------------------------------------------------ */
+/* Methods (plugins "sart", "sirt", "asdpocs", "sbtv").                      */
+/* Each *_process call is the method's UfoTask process: the sinogram(s) in, */
+/* the n_dets x n_dets reconstruction(s) out, starting from x = 0 as the    */
+/* reference does. The projector's geometry comes from the sinogram dims    */
+/* (n_dets = dims[0], n_angles = angles_num or dims[1]) as in               */
+/* src/core/ufo-ir-method-task.c:241-252. Methods leave the projector's     */
+/* relaxation / correction_scale properties where the reference leaves them.*/
+/* ------------------------------------------------------------------------ */
+
+/* Norm arithmetic for the host-side reductions of ASD-POCS and SBTV.
+ * COMPAT: float, sequential, in the reference's order (bit-identical to the
+ *         reference's host loops; slow - one thread per sum).
+ * FP64:   the same terms accumulated in double by a deterministic parallel
+ *         reduction, rounded to float (default). */
+enum { UFOIR_NORM_COMPAT = 0, UFOIR_NORM_FP64 = 1 };
+
+/* "num-iterations" [1, MAX] default 10 (src/core/ufo-ir-method-task.c:75-80);
+ * "relaxation_factor" [0, 1] default 0.25 (src/tasks/ufo-ir-sart-task.c:76-81,
+ * src/tasks/ufo-ir-sirt-task.c:73-77). */
+typedef struct {
+    unsigned int num_iterations;
+    float relaxation_factor;
+} ufoir_sart_params;
+typedef ufoir_sart_params ufoir_sirt_params;
+
+/* src/tasks/ufo-ir-asdpocs-task.c:104-181. ng is accepted and ignored, as in
+ * the reference (20 TV sub-steps are hard-coded at :573). df_minimizer holds
+ * the nested SART node's properties. */
+typedef struct {
+    unsigned int num_iterations;   /* outer iterations, default 10 */
+    float beta;                    /* [0, MAX] 1.0 */
+    float beta_red;                /* [0, MAX] 0.995 */
+    float alpha;                   /* [0, MAX] 0.2 */
+    float alpha_red;               /* [0, MAX] 0.95 */
+    float r_max;                   /* [0, MAX] 0.95 */
+    unsigned int ng;               /* [0, 1000] 20 (unused) */
+    int positive_constraint;       /* TRUE */
+    ufoir_sart_params df_minimizer;
+    int norm_mode;                 /* UFOIR_NORM_FP64 */
+} ufoir_asdpocs_params;
+
+/* src/tasks/ufo-ir-sbtv-task.c:90-116: lambda [0, MAX] 0.1, mu [0, MAX] 0.5. */
+typedef struct {
+    unsigned int num_iterations;
+    float lambda;
+    float mu;
+    int norm_mode;                 /* UFOIR_NORM_FP64 */
+} ufoir_sbtv_params;
+
+UFOIR_API void ufoir_sart_params_init(ufoir_sart_params *p);
+UFOIR_API void ufoir_sirt_params_init(ufoir_sirt_params *p);
+UFOIR_API void ufoir_asdpocs_params_init(ufoir_asdpocs_params *p);
+UFOIR_API void ufoir_sbtv_params_init(ufoir_sbtv_params *p);
+
+/* SART: src/tasks/ufo-ir-sart-task.c:173-228. */
+UFOIR_API int ufoir_sart_process(ufoir_projector *proj, const ufoir_sart_params *p,
+                                 const float *sino, const size_t sino_dims[2], float *vol,
+                                 size_t n_slices);
+/* SIRT: src/tasks/ufo-ir-sirt-task.c:164-222. n_slices > 1 runs the batched
+ * form: one FP and one BP launch per iteration for all slices, the whole
+ * iteration loop captured in one CUDA graph. */
+UFOIR_API int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *p,
+                                 const float *sino, const size_t sino_dims[2], float *vol,
+                                 size_t n_slices);
+/* ASD-POCS: src/tasks/ufo-ir-asdpocs-task.c:411-580. */
+UFOIR_API int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *p,
+                                    const float *sino, const size_t sino_dims[2], float *vol,
+                                    size_t n_slices);
+/* Split-Bregman TV: src/tasks/ufo-ir-sbtv-task.c:230-635. The reference
+ * min-max-normalises its input sinogram in place (:239); this call leaves
+ * the caller's sinogram untouched and works on a normalised copy. */
+UFOIR_API int ufoir_sbtv_process(ufoir_projector *proj, const ufoir_sbtv_params *p,
+                                 const float *sino, const size_t sino_dims[2], float *vol,
+                                 size_t n_slices);
+
+/* ------------------------------------------------------------------------ */
+/* Resident batched SIRT: the persistent form of ufoir_sirt_process for     */
+/* many slices whose data stay in HBM. Creation computes the weights (once, */
+/* shared by all slices), zeroes the volumes and captures one iteration     */
+/* (transpose + FP + BP launches over all slices) as a CUDA graph; run()    */
+/* replays it. Results equal ufoir_sirt_process with the same iteration     */
+/* count, bit for bit. No reference counterpart beyond sirt-task.c:164-222: */
+/* it splits that process() into setup and iterations.                      */
+/* ------------------------------------------------------------------------ */
+typedef struct ufoir_sirt_batch ufoir_sirt_batch;
+
+/* d_sino: n_slices sinograms in device memory; d_vol: n_slices output
+ * volumes in device memory (zeroed here). Both must stay valid until destroy. */
+UFOIR_API int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *p,
+                                      const float *d_sino, const size_t sino_dims[2], float *d_vol,
+                                      size_t n_slices, ufoir_sirt_batch **out);
+/* Advance every slice by `iterations` SIRT iterations (synchronous). */
+UFOIR_API int ufoir_sirt_batch_run(ufoir_sirt_batch *b, unsigned int iterations);
+/* Restart from x = 0. */
+UFOIR_API int ufoir_sirt_batch_reset(ufoir_sirt_batch *b);
+/* Run one iteration eagerly with CUDA events around each launch on the
+ * context's stream; ms[0..2] = transpose, forward projection, backprojection
+ * durations in milliseconds. The iteration counts toward the result. */
+UFOIR_API int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3]);
+UFOIR_API void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b);
+
+/* ------------------------------------------------------------------------ */
+/* Reductions used by the methods, exposed for callers and tests.           */
+/* ufo_ir_op_l1_norm (src/core/ufo-ir-basic-ops.c:259-277) and              */
+/* ufo_ir_basic_ops_processor_dot_product (src/core/ufo-ir-basic-ops-processor.c:148-196, */
+/* including its index expression partNum * i at :189). w = dims[0],        */
+/* h = dims[1]. Results are written to *out (host).                          */
+/* ------------------------------------------------------------------------ */
+UFOIR_API int ufoir_l1_norm(ufoir_ctx *ctx, const float *v, size_t w, size_t h, int norm_mode,
+                            float *out);
+UFOIR_API int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, size_t w,
+                                size_t h, int norm_mode, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -220,6 +220,25 @@ void oracle_sirt(const oracle_kernels *k, oracle_projector *p, unsigned int iter
     sirt_impl_f(k, p, iters, relaxation_factor, sino, vol);
 }
 
+void oracle_sirt_weights(const oracle_kernels *k, oracle_projector *p, float *ray_weights,
+                         float *pixel_weights)
+{
+    geom_f g;
+    geom_init_f(&g, p);
+    sirt_weights_f(k, p, &g, ray_weights, pixel_weights);
+    geom_free_f(&g);
+}
+
+void oracle_sirt_iterate(const oracle_kernels *k, oracle_projector *p, unsigned int iters,
+                         float relaxation_factor, const float *sino, float *ray_weights,
+                         float *pixel_weights, float *vol)
+{
+    geom_f g;
+    geom_init_f(&g, p);
+    sirt_iterate_f(k, p, &g, iters, relaxation_factor, sino, ray_weights, pixel_weights, vol);
+    geom_free_f(&g);
+}
+
 void oracle_asdpocs(const oracle_kernels *k, oracle_projector *p, const oracle_asdpocs_params *prm,
                     const float *sino, float *vol, float *x_internal)
 {

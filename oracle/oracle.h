@@ -146,6 +146,14 @@ void oracle_sart(const oracle_kernels *k, oracle_projector *p, unsigned int iter
 void oracle_sirt(const oracle_kernels *k, oracle_projector *p, unsigned int iters,
                  float relaxation_factor, const float *sino, float *vol);
 
+/* SIRT split into its weight computation (sirt-task.c:176-193) and the
+ * iteration loop (:201-215) continuing from vol; used to time one iteration. */
+void oracle_sirt_weights(const oracle_kernels *k, oracle_projector *p, float *ray_weights,
+                         float *pixel_weights);
+void oracle_sirt_iterate(const oracle_kernels *k, oracle_projector *p, unsigned int iters,
+                         float relaxation_factor, const float *sino, float *ray_weights,
+                         float *pixel_weights, float *vol);
+
 typedef struct {
     unsigned int num_iterations;   /* outer iterations, method-task default 10 */
     float beta, beta_red, alpha, alpha_red, r_max;

@@ -132,6 +132,8 @@ def _declare(lib):
     lib.oracle_projector_process.argtypes = [kp, pp, C.c_int, f32p, f32p]
     lib.oracle_sart.argtypes = [kp, pp, C.c_uint, C.c_float, f32p, f32p]
     lib.oracle_sirt.argtypes = [kp, pp, C.c_uint, C.c_float, f32p, f32p]
+    lib.oracle_sirt_weights.argtypes = [kp, pp, f32p, f32p]
+    lib.oracle_sirt_iterate.argtypes = [kp, pp, C.c_uint, C.c_float, f32p, f32p, f32p, f32p]
     lib.oracle_asdpocs.argtypes = [kp, pp, C.POINTER(AsdpocsParams), f32p, f32p, f32p]
     lib.oracle_sbtv.argtypes = [kp, pp, C.POINTER(SbtvParams), f32p, f32p]
     for name in ("oracle_l1_norm", "oracle_l1_norm_fp64"):
@@ -213,6 +215,14 @@ def backward(p: Projector, sino, vol=None, which="port"):
     return vol
 
 
+def projector_process(p: Projector, is_forward: bool, inp, which="port"):
+    """State-dependent process: zero the output, then forward or backward."""
+    shape = (p.n_angles, p.n_dets) if is_forward else (p.n_dets, p.n_dets)
+    out = np.zeros(shape, np.float32)
+    port_lib().oracle_projector_process(kernels(which), C.byref(p), int(bool(is_forward)), _f32(inp), _f32(out))
+    return out
+
+
 def sart(p: Projector, sino, iters, relaxation=0.25, which="port"):
     vol = np.zeros((p.n_dets, p.n_dets), np.float32)
     port_lib().oracle_sart(kernels(which), C.byref(p), iters, relaxation, _f32(sino), _f32(vol))
@@ -222,6 +232,20 @@ def sart(p: Projector, sino, iters, relaxation=0.25, which="port"):
 def sirt(p: Projector, sino, iters, relaxation=0.25, which="port"):
     vol = np.zeros((p.n_dets, p.n_dets), np.float32)
     port_lib().oracle_sirt(kernels(which), C.byref(p), iters, relaxation, _f32(sino), _f32(vol))
+    return vol
+
+
+def sirt_weights(p: Projector, which="port"):
+    R = np.zeros((p.n_angles, p.n_dets), np.float32)
+    Cw = np.zeros((p.n_dets, p.n_dets), np.float32)
+    port_lib().oracle_sirt_weights(kernels(which), C.byref(p), _f32(R), _f32(Cw))
+    return R, Cw
+
+
+def sirt_iterate(p: Projector, sino, R, Cw, vol, iters=1, relaxation=0.25, which="port"):
+    """Continue SIRT from vol (in place) for iters iterations."""
+    port_lib().oracle_sirt_iterate(kernels(which), C.byref(p), iters, relaxation, _f32(sino), _f32(R),
+                                   _f32(Cw), _f32(vol))
     return vol
 
 

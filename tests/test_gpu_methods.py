@@ -1,0 +1,159 @@
+"""GPU parity of SART, SIRT, ASD-POCS and split-Bregman TV through the C ABI.
+
+Tolerance (the benchmark spec): relative L2 error <= 1e-4 after the stated number of
+iterations. In COMPAT norm mode every operation, including the host-side
+float sums, is the reference's, so results are also required to be equal
+bit for bit to the oracle and to the golden fixtures.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL_ITER = 1e-4
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def _method_proj(ufoir, ctx, step, axis=-1.0):
+    return ufoir.ParallelProjector(ctx, step=float(step), axis_position=float(axis), is_forward=0)
+
+
+@pytest.mark.parametrize("n,na,axis,iters,slices", [(16, 12, -1.0, 5, 1), (33, 40, 15.3, 4, 3),
+                                                     (64, 90, -1.0, 3, 2), (100, 60, 48.75, 3, 1)])
+def test_sirt_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
+    rng = np.random.default_rng(n * na)
+    step = np.float32(np.pi / na)
+    sinos = rng.random((slices, na, n), dtype=np.float32) * n
+    p = _method_proj(ufoir_lib, gpu_ctx, step, axis)
+    got = ufoir_lib.sirt(p, sinos, num_iterations=iters, relaxation_factor=0.25)
+    for i in range(slices):
+        want = oracle.sirt(oracle.projector(n, na, step, axis), sinos[i], iters, 0.25)
+        assert rel_l2(got[i], want) <= TOL_ITER
+        assert np.array_equal(got[i], want), (i, np.abs(got[i] - want).max())
+    # the reference leaves relaxation = lambda and correction_scale = -1 on the projector
+    assert p.params.relaxation == np.float32(0.25) and p.params.correction_scale == -1.0
+
+
+@pytest.mark.parametrize("n,na,axis,iters,slices", [(16, 12, -1.0, 2, 1), (33, 40, 15.3, 2, 2),
+                                                     (48, 36, -1.0, 1, 1)])
+def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
+    rng = np.random.default_rng(3 * n + na)
+    step = np.float32(np.pi / na)
+    sinos = rng.random((slices, na, n), dtype=np.float32) * n
+    p = _method_proj(ufoir_lib, gpu_ctx, step, axis)
+    got = ufoir_lib.sart(p, sinos, num_iterations=iters, relaxation_factor=0.3)
+    for i in range(slices):
+        want = oracle.sart(oracle.projector(n, na, step, axis), sinos[i], iters, 0.3)
+        assert rel_l2(got[i], want) <= TOL_ITER
+        assert np.array_equal(got[i], want), (i, np.abs(got[i] - want).max())
+
+
+def test_methods_golden_fixture_compat(ufoir_lib, gpu_ctx):
+    d = np.load(os.path.join(GOLDEN, "methods_n20_a18.npz"))
+    step = np.float32(d["step"])
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    got = ufoir_lib.asdpocs(p, d["sino"], num_iterations=3, norm_mode=ufoir_lib.NORM_COMPAT,
+                            df_minimizer=dict(num_iterations=2, relaxation_factor=0.25))
+    assert rel_l2(got, d["asdpocs"]) <= TOL_ITER and np.array_equal(got, d["asdpocs"])
+    p2 = _method_proj(ufoir_lib, gpu_ctx, step)
+    u = ufoir_lib.sbtv(p2, d["sino"], num_iterations=2, norm_mode=ufoir_lib.NORM_COMPAT, mu=1.0,
+                       **{"lambda": 0.05})
+    assert rel_l2(u, d["sbtv"]) <= TOL_ITER
+    assert np.array_equal(u, d["sbtv"]), np.abs(u - d["sbtv"]).max()
+    assert np.float32(gpu_ctx.l1_norm(d["a"], ufoir_lib.NORM_COMPAT)) == d["l1"]
+    assert np.float32(gpu_ctx.dot_product(d["a"], d["b"], ufoir_lib.NORM_COMPAT)) == d["dot"]
+
+
+@pytest.mark.parametrize("mode", ["compat", "fp64"])
+def test_asdpocs_matches_oracle(ufoir_lib, gpu_ctx, oracle, mode):
+    n, na = 40, 30
+    rng = np.random.default_rng(21)
+    step = np.float32(np.pi / na)
+    vol = rng.random((n, n), dtype=np.float32)
+    sino = oracle.forward(oracle.projector(n, na, step), vol)
+    m = ufoir_lib.NORM_COMPAT if mode == "compat" else ufoir_lib.NORM_FP64
+    om = oracle.NORM_COMPAT if mode == "compat" else oracle.NORM_FP64
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    got = ufoir_lib.asdpocs(p, np.stack([sino, sino * 0.5]), num_iterations=3, norm_mode=m,
+                            df_minimizer=dict(num_iterations=2, relaxation_factor=0.25))
+    prm = oracle.asdpocs_params(num_iterations=3, sart_iterations=2, norm_mode=om)
+    want, _ = oracle.asdpocs(oracle.projector(n, na, step), sino, prm)
+    want2, _ = oracle.asdpocs(oracle.projector(n, na, step), sino * 0.5, prm)
+    assert rel_l2(got[0], want) <= TOL_ITER and rel_l2(got[1], want2) <= TOL_ITER
+    assert np.array_equal(got[0], want) and np.array_equal(got[1], want2)
+    wd, _ = oracle.asdpocs_d(oracle.projector(n, na, step), sino, prm)
+    assert rel_l2(got[0], wd) < 1e-4       # error against the FP64 recomputation
+
+
+@pytest.mark.parametrize("mode", ["compat", "fp64"])
+def test_sbtv_matches_oracle(ufoir_lib, gpu_ctx, oracle, mode):
+    n, na = 32, 24
+    rng = np.random.default_rng(33)
+    step = np.float32(np.pi / na)
+    vol = rng.random((n, n), dtype=np.float32)
+    sino = oracle.forward(oracle.projector(n, na, step), vol)
+    m = ufoir_lib.NORM_COMPAT if mode == "compat" else ufoir_lib.NORM_FP64
+    om = oracle.NORM_COMPAT if mode == "compat" else oracle.NORM_FP64
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    keep = sino.copy()
+    got = ufoir_lib.sbtv(p, sino, num_iterations=2, norm_mode=m, mu=1.0, **{"lambda": 0.05})
+    assert np.array_equal(sino, keep)        # the caller's sinogram is left untouched
+    prm = oracle.sbtv_params(num_iterations=2, lambda_=0.05, mu=1.0, norm_mode=om)
+    want, _ = oracle.sbtv(oracle.projector(n, na, step), sino, prm)
+    assert rel_l2(got, want) <= TOL_ITER
+    if mode == "compat":
+        assert np.array_equal(got, want), np.abs(got - want).max()
+    wd = oracle.sbtv_d(oracle.projector(n, na, step), sino, prm)
+    assert rel_l2(got, wd) < 1e-3
+
+
+def test_norms_match_oracle(ufoir_lib, gpu_ctx, oracle):
+    rng = np.random.default_rng(5)
+    for h, w in [(1, 1), (7, 13), (64, 64), (300, 257)]:
+        a = rng.standard_normal((h, w)).astype(np.float32)
+        b = rng.standard_normal((h, w)).astype(np.float32)
+        assert np.float32(gpu_ctx.l1_norm(a, ufoir_lib.NORM_COMPAT)) == np.float32(oracle.l1_norm(a))
+        assert np.float32(gpu_ctx.dot_product(a, b, ufoir_lib.NORM_COMPAT)) == np.float32(oracle.dot_product(a, b))
+        assert abs(gpu_ctx.l1_norm(a) - oracle.l1_norm(a, fp64=True)) <= 1e-6 * oracle.l1_norm(a, fp64=True)
+        d64 = oracle.dot_product(a, b, fp64=True)
+        assert abs(gpu_ctx.dot_product(a, b) - d64) <= 1e-6 * (abs(d64) + 1)
+
+
+def test_c1_sart_full_size(ufoir_lib, gpu_ctx, oracle):
+    # SART on the 367-bin, 180-angle geometry with a 256^2 phantom (2 iterations).
+    from ufoir import synth
+    n, na = 367, 180
+    step = np.float32(np.pi / na)
+    vol = synth.ellipse_phantom(n, 256, 10, seed=1001)
+    sino = oracle.forward(oracle.projector(n, na, step), vol)
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    got = ufoir_lib.sart(p, sino, num_iterations=2, relaxation_factor=0.25)
+    want = oracle.sart(oracle.projector(n, na, step), sino, 2, 0.25)
+    assert rel_l2(got, want) <= TOL_ITER and np.array_equal(got, want)
+
+
+def test_method_argument_errors(ufoir_lib, gpu_ctx):
+    p = ufoir_lib.ParallelProjector(gpu_ctx, step=0.1)          # is_forward defaults to TRUE
+    sino = np.ones((10, 16), np.float32)
+    with pytest.raises(ufoir_lib.UfoirError) as e:
+        ufoir_lib.sirt(p, sino)
+    assert e.value.status == ufoir_lib.ERR_INVALID
+    q = _method_proj(ufoir_lib, gpu_ctx, 0.1)
+    with pytest.raises(ufoir_lib.UfoirError):
+        ufoir_lib.sirt(q, sino, relaxation_factor=1.5)
+    with pytest.raises(ufoir_lib.UfoirError):
+        ufoir_lib.sart(q, sino, num_iterations=0)
+    with pytest.raises(ufoir_lib.UfoirError):
+        ufoir_lib.asdpocs(q, sino, ng=5000)
+    out = ufoir_lib.sirt(q, sino, num_iterations=1)
+    assert np.isfinite(out).all()

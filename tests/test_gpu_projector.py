@@ -1,0 +1,211 @@
+"""GPU parity of the projector (FP / BP / process / subsets) through the C ABI.
+
+Tolerance (the benchmark spec): relative L2 error <= 1e-5 after one application.
+The kernels follow the reference's operation order exactly, so the tests
+also require bit equality with the oracle and the golden fixtures (made by
+the reference's own kernel sources) wherever the inputs are identical.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL_ONE = 1e-5
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def _proj(ufoir, ctx, n, na, step, axis=-1.0, **kw):
+    p = ufoir.ParallelProjector(ctx, step=float(step), axis_position=float(axis), **kw)
+    p.get_requisition((n, na))
+    return p
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "proj_*.npz"))),
+                         ids=lambda p: os.path.basename(p)[:-4])
+def test_golden_fixtures(ufoir_lib, gpu_ctx, path):
+    d = np.load(path)
+    n, na, step, axis = int(d["n"]), int(d["na"]), np.float32(d["step"]), float(d["axis"])
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, axis)
+    s, c = p.host_sin_cos()
+    assert np.array_equal(s, d["sin"]) and np.array_equal(c, d["cos"])
+    assert p.subsets() == [tuple(x) for x in d["subsets"].tolist()]
+    sino = p.forward(d["vol"], np.zeros((na, n), np.float32))
+    assert rel_l2(sino, d["fp"]) <= TOL_ONE
+    assert np.array_equal(sino, d["fp"])
+    vol = p.backward(np.zeros((n, n), np.float32), d["fp"])
+    assert rel_l2(vol, d["bp"]) <= TOL_ONE
+    assert np.array_equal(vol, d["bp"])
+    p.set(is_forward=0)
+    x = ufoir_lib.sirt(p, d["fp"], num_iterations=int(d["sirt_iters"]))
+    assert rel_l2(x, d["sirt"]) <= 1e-4 and np.array_equal(x, d["sirt"])
+    x = ufoir_lib.sart(p, d["fp"], num_iterations=int(d["sart_iters"]))
+    assert rel_l2(x, d["sart"]) <= 1e-4 and np.array_equal(x, d["sart"])
+
+
+CASES = [(7, 5, -1.0), (16, 12, -1.0), (33, 40, 15.3), (33, 40, 17.9), (64, 90, -1.0),
+         (100, 180, -1.0), (61, 36, 31.25), (128, 7, -1.0)]
+
+
+@pytest.mark.parametrize("n,na,axis", CASES)
+def test_fp_bp_match_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis):
+    rng = np.random.default_rng(n + 7 * na)
+    step = np.float32(np.pi / na)
+    vols = rng.random((3, n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, axis)
+    op = oracle.projector(n, na, step, axis)
+    # batched (3 slices) accumulate into a non-zero sinogram
+    base = rng.random((3, na, n), dtype=np.float32)
+    got = p.forward(vols, base.copy())
+    for i in range(3):
+        want = oracle.forward(op, vols[i], base[i].copy())
+        assert rel_l2(got[i], want) <= TOL_ONE
+        assert np.array_equal(got[i], want), (i, np.abs(got[i] - want).max())
+    vb = rng.random((3, n, n), dtype=np.float32)
+    gotb = p.backward(vb.copy(), got)
+    for i in range(3):
+        want = oracle.backward(op, got[i], vb[i].copy())
+        assert np.array_equal(gotb[i], want), (i, np.abs(gotb[i] - want).max())
+
+
+def test_properties_scale_and_relaxation(ufoir_lib, gpu_ctx, oracle):
+    n, na = 40, 30
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(5)
+    vol = rng.random((n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, correction_scale=-0.75, relaxation=0.3)
+    op = oracle.projector(n, na, step, -1.0, 0.3, -0.75)
+    b = rng.random((na, n), dtype=np.float32)
+    assert np.array_equal(p.forward(vol, b.copy()), oracle.forward(op, vol, b.copy()))
+    assert np.array_equal(p.backward(vol.copy(), b), oracle.backward(op, b, vol.copy()))
+
+
+def test_process_forward_and_backward(ufoir_lib, gpu_ctx, oracle):
+    n, na = 48, 33
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(9)
+    vol = rng.random((n, n), dtype=np.float32)
+    p = ufoir_lib.ParallelProjector(gpu_ctx, step=float(step), angles_num=na, is_forward=1)
+    sino = p.process(vol)
+    assert sino.shape == (na, n)
+    op = oracle.projector(n, na, step)
+    want = oracle.projector_process(op, True, vol)
+    assert np.array_equal(sino, want)
+    q = ufoir_lib.ParallelProjector(gpu_ctx, step=float(step), is_forward=0)
+    back = q.process(sino)
+    assert back.shape == (n, n)
+    assert np.array_equal(back, oracle.backward(op, sino))
+
+
+def test_subset_fp_bp(ufoir_lib, gpu_ctx, oracle):
+    import ctypes
+    n, na = 36, 24
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(12)
+    vol = rng.random((n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, correction_scale=-1.0, relaxation=0.5)
+    s, c = oracle.lut(na, step)
+    k = oracle.kernels().contents
+    dims = oracle.Dims(n, n, n, na)
+    for (off, cnt, direction) in [(3, 1, 1), (8, 5, 0), (0, 2, 1), (20, 4, 1)]:
+        sino = rng.random((na, n), dtype=np.float32)
+        want = sino.copy()
+        k.fp(oracle.image(vol), oracle.image(want), s.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+             c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), dims, np.float32(n / 2.0),
+             oracle.Subset(off, cnt, direction), np.float32(-1.0))
+        got = p.subset_fp(vol, sino.copy(), off, cnt, direction)
+        assert np.array_equal(got, want)
+        v0 = rng.random((n, n), dtype=np.float32)
+        wantv = v0.copy()
+        k.bp(oracle.image(wantv), oracle.image(sino), np.float32(0.5),
+             s.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), c.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+             dims, np.float32(n / 2.0), oracle.Subset(off, cnt, direction))
+        gotv = p.subset_bp(v0.copy(), sino, off, cnt, direction)
+        assert np.array_equal(gotv, wantv)
+
+
+def test_device_pointers_and_host_pointers_agree(ufoir_lib, gpu_ctx):
+    n, na = 64, 50
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(2)
+    vol = rng.random((2, n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step)
+    host = p.forward(vol, np.zeros((2, na, n), np.float32))
+    dv = ufoir_lib.DeviceArray.from_numpy(gpu_ctx, vol)
+    ds = ufoir_lib.DeviceArray(gpu_ctx, (2, na, n), zero=True)
+    p.forward(dv, ds)
+    assert np.array_equal(ds.download(), host)
+    dv.close()
+    ds.close()
+
+
+def test_full_size_geometry_properties(ufoir_lib, gpu_ctx):
+    # 1448 bins, 1200 angles over [0, pi): the configuration of the headline metric.
+    n, na = 1448, 1200
+    step = np.float32(np.pi / na)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step)
+    ones = ufoir_lib.DeviceArray.from_numpy(gpu_ctx, np.ones((n, n), np.float32))
+    sino = ufoir_lib.DeviceArray(gpu_ctx, (na, n), zero=True)
+    p.forward(ones, sino)
+    s = sino.download()
+    assert np.all(s[0] == n)                     # theta = 0 samples texel centres only
+    rng = np.random.default_rng(4)
+    a = rng.random((n, n), dtype=np.float32)
+    b = rng.random((n, n), dtype=np.float32)
+    fa = p.forward(a, np.zeros((na, n), np.float32))
+    fb = p.forward(b, np.zeros((na, n), np.float32))
+    fab = p.forward(a + b, np.zeros((na, n), np.float32))
+    assert rel_l2(fab, fa + fb) < 1e-6          # linearity up to float rounding
+    # a slice computed inside a batch equals the slice computed alone, bit for bit
+    batch = p.forward(np.stack([b, a]), np.zeros((2, na, n), np.float32))
+    assert np.array_equal(batch[1], fa) and np.array_equal(batch[0], fb)
+    back = p.backward(np.zeros((n, n), np.float32), np.ones((na, n), np.float32))
+    assert np.allclose(back, na, rtol=0, atol=na * 1e-6)
+    ones.close()
+    sino.close()
+
+
+def test_full_size_bp_matches_oracle_on_a_row_band(ufoir_lib, gpu_ctx, oracle):
+    # C1 geometry in full (367 bins, 180 angles), compared with the oracle.
+    n, na = 367, 180
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(8)
+    vol = rng.random((n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step)
+    op = oracle.projector(n, na, step)
+    got = p.forward(vol, np.zeros((na, n), np.float32))
+    want = oracle.forward(op, vol)
+    assert rel_l2(got, want) <= TOL_ONE and np.array_equal(got, want)
+    gb = p.backward(np.zeros((n, n), np.float32), want)
+    wb = oracle.backward(op, want)
+    assert rel_l2(gb, wb) <= TOL_ONE and np.array_equal(gb, wb)
+
+
+def test_errors_are_reported_not_fatal(ufoir_lib, gpu_ctx):
+    with pytest.raises(ufoir_lib.UfoirError) as e:
+        ufoir_lib.ParallelProjector(gpu_ctx, model="siddon")
+    assert e.value.status == ufoir_lib.ERR_UNSUPPORTED
+    with pytest.raises(ufoir_lib.UfoirError) as e:
+        ufoir_lib.ParallelProjector(gpu_ctx, step=-1.0)
+    assert e.value.status == ufoir_lib.ERR_INVALID
+    p = ufoir_lib.ParallelProjector(gpu_ctx, step=0.1)
+    with pytest.raises(ufoir_lib.UfoirError) as e:
+        p.subset_fp(np.zeros((8, 8), np.float32), np.zeros((4, 8), np.float32), 0, 1, 1)
+    assert e.value.status == ufoir_lib.ERR_STATE
+    p.get_requisition((8, 4))
+    with pytest.raises(ufoir_lib.UfoirError) as e:
+        p.subset_fp(np.zeros((8, 8), np.float32), np.zeros((4, 8), np.float32), 3, 2, 1)
+    assert e.value.status == ufoir_lib.ERR_INVALID
+    # the context is still usable
+    out = p.forward(np.ones((8, 8), np.float32), np.zeros((4, 8), np.float32))
+    assert np.isfinite(out).all()

@@ -1,0 +1,72 @@
+/*
+ * host.h - private declarations of the C host library.
+ */
+#ifndef UFOIR_HOST_H
+#define UFOIR_HOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "udev.h"
+#include "ufoir.h"
+
+struct ufoir_ctx {
+    udev *dev;
+    uint64_t hbm_budget;
+    char create_err[256];
+};
+
+struct ufoir_projector {
+    ufoir_ctx *ctx;
+    ufoir_projector_params prm;
+    /* geometry built by the requisition (…parallel-projector-task.c:306-347) */
+    int have_geometry;
+    unsigned int n_dets;
+    unsigned int n_angles;
+    float lut_step;
+    float *h_sin, *h_cos;
+    unsigned char *h_dir;
+    ufoir_subset *subsets;
+    unsigned int n_subsets;
+    float *d_sin, *d_cos;
+    unsigned char *d_dir;
+    unsigned int lut_cap;
+};
+
+/* Error helpers: record a message on the context and return the status. */
+int ufoir__fail(ufoir_ctx *ctx, int status, const char *fmt, ...);
+
+#define UFOIR_TRY(expr)          \
+    do {                         \
+        rc = (expr);             \
+        if (rc != UFOIR_OK)      \
+            goto done;           \
+    } while (0)
+
+/* Resolves the geometry for a sinogram/volume input of dims in_dims, exactly
+ * as get_requisition does, and uploads the LUT when it changes. */
+int ufoir__projector_prepare(ufoir_projector *p, const size_t in_dims[2]);
+/* Same, with explicit detector and angle counts (forward/backward calls). */
+int ufoir__projector_prepare_na(ufoir_projector *p, unsigned int n_dets, unsigned int n_angles);
+/* Device geometry descriptor for the kernels. */
+void ufoir__projector_geom(const ufoir_projector *p, udev_geom *g);
+/* Axis position with the -1 default resolved to n_dets / 2.0. */
+float ufoir__axis(const ufoir_projector *p);
+
+/* Host-or-device staging of a user buffer. */
+typedef struct {
+    float *dev;          /* device pointer used by kernels */
+    float *user;         /* caller's pointer */
+    size_t count;        /* floats */
+    int owned;           /* 1 if dev was allocated here (user is host memory) */
+} ufoir_buf;
+
+int ufoir__buf_in(ufoir_ctx *ctx, ufoir_buf *b, const float *user, size_t count, int copy_in);
+/* Copies back to the user (if host) when copy_out, and releases. */
+int ufoir__buf_out(ufoir_ctx *ctx, ufoir_buf *b, int copy_out);
+void ufoir__buf_release(ufoir_ctx *ctx, ufoir_buf *b);
+
+int ufoir__alloc(ufoir_ctx *ctx, float **p, size_t count);
+void ufoir__free(ufoir_ctx *ctx, void *p);
+
+#endif

@@ -1,0 +1,965 @@
+/*
+ * methods.c - SART, SIRT, ASD-POCS and split-Bregman TV on the GPU.
+ *
+ * Each method follows its reference host loop step for step (the same
+ * buffers, the same operation order, the same float scalar arithmetic), with
+ * runs of element-wise work fused into the projector kernels:
+ *   SIRT iteration  = transpose(x) + FP[(b - Ax) * R] + BP[x + C * (lambda A^T r)]
+ *   SART angle step = FP_theta[(b - A_theta x) * R_theta] + BP_theta[x + lambda A_theta^T r]
+ * The weights R = inv(FP(1)) and C = inv(BP(1)) depend on the geometry only,
+ * so they are computed once per call and shared by all slices.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "host.h"
+
+/* Captured iterations per CUDA graph (bounds graph size for long runs). */
+#define GRAPH_CHUNK 64
+
+void ufoir_sart_params_init(ufoir_sart_params *p)
+{
+    if (!p)
+        return;
+    p->num_iterations = 10;        /* ufo-ir-method-task.c:111 */
+    p->relaxation_factor = 0.25f;  /* ufo-ir-sart-task.c:93 */
+}
+
+void ufoir_sirt_params_init(ufoir_sirt_params *p)
+{
+    if (!p)
+        return;
+    p->num_iterations = 10;
+    p->relaxation_factor = 0.25f;  /* ufo-ir-sirt-task.c:88 */
+}
+
+void ufoir_asdpocs_params_init(ufoir_asdpocs_params *p)
+{
+    if (!p)
+        return;
+    p->num_iterations = 10;
+    p->beta = 1.0f;                /* ufo-ir-asdpocs-task.c:171-180 */
+    p->beta_red = 0.995f;
+    p->ng = 20;
+    p->alpha = 0.2f;
+    p->alpha_red = 0.95f;
+    p->r_max = 0.95f;
+    p->positive_constraint = 1;
+    ufoir_sart_params_init(&p->df_minimizer);
+    p->norm_mode = UFOIR_NORM_FP64;
+}
+
+void ufoir_sbtv_params_init(ufoir_sbtv_params *p)
+{
+    if (!p)
+        return;
+    p->num_iterations = 10;
+    p->lambda = 0.1f;              /* ufo-ir-sbtv-task.c:114-115 */
+    p->mu = 0.5f;
+    p->norm_mode = UFOIR_NORM_FP64;
+}
+
+/* Shared validation + geometry for all methods. */
+static int method_setup(ufoir_projector *proj, const size_t dims[2], size_t n_slices, unsigned int iters)
+{
+    ufoir_ctx *ctx = proj->ctx;
+    if (n_slices == 0)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "n_slices must be >= 1");
+    if (iters < 1)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "num-iterations must be >= 1");
+    if (proj->prm.is_forward)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID,
+                           "a method's projector must have is_forward = false (the method's output is the "
+                           "projector's backward requisition)");
+    int rc = ufoir__projector_prepare(proj, dims);
+    if (rc)
+        return rc;
+    if (dims[1] != proj->n_angles)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "angles_num %u does not match the sinogram's %zu rows",
+                           proj->n_angles, dims[1]);
+    return UFOIR_OK;
+}
+
+static int check_relax(ufoir_ctx *ctx, float r)
+{
+    if (!(r >= 0.0f && r <= 1.0f))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "relaxation_factor %g outside [0, 1]", (double) r);
+    return UFOIR_OK;
+}
+
+/* R = inv(FP(1)) over all angles for one slice (sirt-task.c:180-185,
+ * sart-task.c:193-200). `ones` is scratch of n*n floats. */
+static int ray_weights(ufoir_projector *p, float *R, float *ones)
+{
+    ufoir_ctx *ctx = p->ctx;
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    const size_t n = p->n_dets, nv = n * n, ns = n * p->n_angles;
+    int rc = udev_fill(ctx->dev, ones, nv, 1.0f);
+    if (!rc)
+        rc = udev_fill(ctx->dev, R, ns, 0.0f);
+    /* the transpose of a constant image is itself */
+    if (!rc)
+        rc = udev_fp(ctx->dev, &g, 0, (int) p->n_angles, -1, ones, ones, R, NULL, 0, R, 1.0f, 1);
+    if (!rc)
+        rc = udev_unary(ctx->dev, UDEV_INV, R, 0, 0, R, ns);
+    return rc;
+}
+
+/* C = inv(BP(1)) for one slice (sirt-task.c:188-193). `ones` holds ns floats. */
+static int pixel_weights(ufoir_projector *p, float *C, float *ones)
+{
+    ufoir_ctx *ctx = p->ctx;
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    const size_t n = p->n_dets, nv = n * n, ns = n * p->n_angles;
+    int rc = udev_fill(ctx->dev, ones, ns, 1.0f);
+    if (!rc)
+        rc = udev_bp(ctx->dev, &g, p->subsets, (int) p->n_subsets, ones, NULL, NULL, 0, NULL, C, 1.0f, 1);
+    if (!rc)
+        rc = udev_unary(ctx->dev, UDEV_INV, C, 0, 0, C, nv);
+    return rc;
+}
+
+/* Runs `iters` repetitions of a captured body, GRAPH_CHUNK per graph. */
+typedef int (*body_fn)(void *arg);
+
+static int run_graphed(ufoir_ctx *ctx, unsigned int iters, body_fn body, void *arg)
+{
+    int rc = UFOIR_OK;
+    unsigned int remaining = iters;
+    void *exec = NULL;
+    unsigned int exec_len = 0;
+    uint64_t exec_kernels = 0;
+    while (remaining > 0) {
+        const unsigned int len = remaining >= GRAPH_CHUNK ? GRAPH_CHUNK : remaining;
+        if (!exec || exec_len != len) {
+            udev_graph_destroy(exec);
+            exec = NULL;
+            rc = udev_capture_begin(ctx->dev);
+            if (rc)
+                return rc;
+            for (unsigned int i = 0; i < len && rc == UFOIR_OK; i++)
+                rc = body(arg);
+            void *e = NULL;
+            const int rc2 = udev_capture_end(ctx->dev, &e, &exec_kernels);
+            if (rc || rc2) {
+                udev_graph_destroy(e);
+                return rc ? rc : rc2;
+            }
+            exec = e;
+            exec_len = len;
+        }
+        rc = udev_graph_launch(ctx->dev, exec, exec_kernels);
+        if (rc)
+            break;
+        remaining -= len;
+    }
+    if (rc == UFOIR_OK)
+        rc = udev_sync(ctx->dev);
+    udev_graph_destroy(exec);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* SIRT                                                                     */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    ufoir_projector *p;
+    udev_geom g;
+    const float *b;
+    float *x, *xT, *resid;
+    const float *R, *C;
+    float lambda;
+    int n_slices;
+} sirt_iter;
+
+static int sirt_body(void *arg)
+{
+    sirt_iter *s = (sirt_iter *) arg;
+    udev *d = s->p->ctx->dev;
+    const int n = (int) s->p->n_dets;
+    /* sirt-task.c:202-213: r = (b - A x) * R;  x = x + C * (lambda A^T r) */
+    int rc = udev_transpose(d, s->x, s->xT, n, s->n_slices);
+    if (!rc)
+        rc = udev_fp(d, &s->g, 0, (int) s->p->n_angles, -1, s->x, s->xT, s->b, s->R, 1, s->resid, -1.0f,
+                     s->n_slices);
+    if (!rc)
+        rc = udev_bp(d, &s->g, s->p->subsets, (int) s->p->n_subsets, s->resid, NULL, s->C, 1, s->x, s->x,
+                     s->lambda, s->n_slices);
+    return rc;
+}
+
+int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, const float *sino,
+                       const size_t dims[2], float *vol, size_t n_slices)
+{
+    if (!proj || !prm || !sino || !vol || !dims)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc = check_relax(ctx, prm->relaxation_factor);
+    if (rc)
+        return rc;
+    rc = method_setup(proj, dims, n_slices, prm->num_iterations);
+    if (rc)
+        return rc;
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    ufoir_buf bb = {0}, bx = {0};
+    float *R = NULL, *C = NULL, *xT = NULL, *resid = NULL;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
+    UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
+    UFOIR_TRY(ufoir__alloc(ctx, &C, nv));
+    UFOIR_TRY(ufoir__alloc(ctx, &xT, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices));
+
+    /* weights with relaxation 1 and correction scale 1 (sirt-task.c:176-193) */
+    proj->prm.relaxation = 1.0f;
+    proj->prm.correction_scale = 1.0f;
+    UFOIR_TRY(ray_weights(proj, R, xT));
+    UFOIR_TRY(pixel_weights(proj, C, resid));
+    proj->prm.relaxation = prm->relaxation_factor;
+    proj->prm.correction_scale = -1.0f;
+    UFOIR_TRY(udev_fill(ctx->dev, bx.dev, nv * n_slices, 0.0f));
+
+    sirt_iter it;
+    it.p = proj;
+    ufoir__projector_geom(proj, &it.g);
+    it.b = bb.dev;
+    it.x = bx.dev;
+    it.xT = xT;
+    it.resid = resid;
+    it.R = R;
+    it.C = C;
+    it.lambda = prm->relaxation_factor;
+    it.n_slices = (int) n_slices;
+    UFOIR_TRY(run_graphed(ctx, prm->num_iterations, sirt_body, &it));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
+done:
+    ufoir__free(ctx, R);
+    ufoir__free(ctx, C);
+    ufoir__free(ctx, xT);
+    ufoir__free(ctx, resid);
+    ufoir__buf_release(ctx, &bb);
+    ufoir__buf_release(ctx, &bx);
+    if (rc == UFOIR_OK)
+        rc = udev_sync(ctx->dev);
+    else
+        udev_sync(ctx->dev);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Resident batched SIRT                                                    */
+/* ------------------------------------------------------------------------ */
+struct ufoir_sirt_batch {
+    ufoir_projector *proj;
+    sirt_iter it;
+    float *R, *C, *xT, *resid;
+    size_t nv;
+    void *exec;
+    uint64_t exec_kernels;
+};
+
+void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b)
+{
+    if (!b)
+        return;
+    ufoir_ctx *ctx = b->proj->ctx;
+    udev_sync(ctx->dev);
+    udev_graph_destroy(b->exec);
+    ufoir__free(ctx, b->R);
+    ufoir__free(ctx, b->C);
+    ufoir__free(ctx, b->xT);
+    ufoir__free(ctx, b->resid);
+    udev_sync(ctx->dev);
+    free(b);
+}
+
+int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *prm, const float *d_sino,
+                            const size_t dims[2], float *d_vol, size_t n_slices, ufoir_sirt_batch **out)
+{
+    if (!proj || !prm || !d_sino || !d_vol || !dims || !out)
+        return UFOIR_ERR_INVALID;
+    *out = NULL;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc = check_relax(ctx, prm->relaxation_factor);
+    if (rc)
+        return rc;
+    rc = method_setup(proj, dims, n_slices, 1);
+    if (rc)
+        return rc;
+    if (!udev_is_device_ptr(ctx->dev, d_sino) || !udev_is_device_ptr(ctx->dev, d_vol))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "sirt batch: sinograms and volumes must be device memory");
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    ufoir_sirt_batch *b = (ufoir_sirt_batch *) calloc(1, sizeof(*b));
+    if (!b)
+        return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+    b->proj = proj;
+    b->nv = nv;
+    UFOIR_TRY(ufoir__alloc(ctx, &b->R, ns));
+    UFOIR_TRY(ufoir__alloc(ctx, &b->C, nv));
+    UFOIR_TRY(ufoir__alloc(ctx, &b->xT, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &b->resid, ns * n_slices));
+    proj->prm.relaxation = 1.0f;
+    proj->prm.correction_scale = 1.0f;
+    UFOIR_TRY(ray_weights(proj, b->R, b->xT));
+    UFOIR_TRY(pixel_weights(proj, b->C, b->resid));
+    proj->prm.relaxation = prm->relaxation_factor;
+    proj->prm.correction_scale = -1.0f;
+    UFOIR_TRY(udev_fill(ctx->dev, d_vol, nv * n_slices, 0.0f));
+    b->it.p = proj;
+    ufoir__projector_geom(proj, &b->it.g);
+    b->it.b = d_sino;
+    b->it.x = d_vol;
+    b->it.xT = b->xT;
+    b->it.resid = b->resid;
+    b->it.R = b->R;
+    b->it.C = b->C;
+    b->it.lambda = prm->relaxation_factor;
+    b->it.n_slices = (int) n_slices;
+    UFOIR_TRY(udev_capture_begin(ctx->dev));
+    rc = sirt_body(&b->it);
+    {
+        const int rc2 = udev_capture_end(ctx->dev, &b->exec, &b->exec_kernels);
+        if (!rc)
+            rc = rc2;
+    }
+    if (rc)
+        goto done;
+    UFOIR_TRY(udev_sync(ctx->dev));
+    *out = b;
+    return UFOIR_OK;
+done:
+    ufoir_sirt_batch_destroy(b);
+    return rc;
+}
+
+int ufoir_sirt_batch_run(ufoir_sirt_batch *b, unsigned int iterations)
+{
+    if (!b)
+        return UFOIR_ERR_INVALID;
+    udev *d = b->proj->ctx->dev;
+    for (unsigned int i = 0; i < iterations; i++) {
+        int rc = udev_graph_launch(d, b->exec, b->exec_kernels);
+        if (rc)
+            return rc;
+    }
+    return udev_sync(d);
+}
+
+int ufoir_sirt_batch_reset(ufoir_sirt_batch *b)
+{
+    if (!b)
+        return UFOIR_ERR_INVALID;
+    udev *d = b->proj->ctx->dev;
+    int rc = udev_fill(d, b->it.x, b->nv * (size_t) b->it.n_slices, 0.0f);
+    return rc ? rc : udev_sync(d);
+}
+
+int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3])
+{
+    if (!b || !ms)
+        return UFOIR_ERR_INVALID;
+    sirt_iter *s = &b->it;
+    udev *d = s->p->ctx->dev;
+    const int n = (int) s->p->n_dets;
+    int rc;
+    if ((rc = udev_timer_begin(d)) || (rc = udev_transpose(d, s->x, s->xT, n, s->n_slices)) ||
+        (rc = udev_timer_end(d, &ms[0])))
+        return rc;
+    if ((rc = udev_timer_begin(d)) ||
+        (rc = udev_fp(d, &s->g, 0, (int) s->p->n_angles, -1, s->x, s->xT, s->b, s->R, 1, s->resid, -1.0f,
+                      s->n_slices)) ||
+        (rc = udev_timer_end(d, &ms[1])))
+        return rc;
+    if ((rc = udev_timer_begin(d)) ||
+        (rc = udev_bp(d, &s->g, s->p->subsets, (int) s->p->n_subsets, s->resid, NULL, s->C, 1, s->x, s->x,
+                      s->lambda, s->n_slices)) ||
+        (rc = udev_timer_end(d, &ms[2])))
+        return rc;
+    return UFOIR_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* SART                                                                     */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    ufoir_projector *p;
+    udev_geom g;
+    const float *b;
+    float *x, *resid;
+    const float *R;
+    float lambda;
+    int n_slices;
+} sart_iter;
+
+static int sart_body(void *arg)
+{
+    sart_iter *s = (sart_iter *) arg;
+    udev *d = s->p->ctx->dev;
+    int rc = UFOIR_OK;
+    /* sart-task.c:209-217: per angle, r_theta = (b_theta - A_theta x) * R_theta;
+     * x = x + lambda A_theta^T r_theta. */
+    for (unsigned int a = 0; a < s->p->n_angles && rc == UFOIR_OK; a++) {
+        ufoir_subset sub;
+        sub.offset = a;
+        sub.n = 1;
+        sub.direction = s->p->h_dir[a];
+        rc = udev_fp(d, &s->g, (int) a, 1, sub.direction, s->x, NULL, s->b, s->R, 1, s->resid, -1.0f,
+                     s->n_slices);
+        if (!rc)
+            rc = udev_bp(d, &s->g, &sub, 1, s->resid, s->x, NULL, 0, NULL, s->x, s->lambda, s->n_slices);
+    }
+    return rc;
+}
+
+/* One SART call on resident buffers: x = SART(b), R precomputed. */
+static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, const float *b, float *x,
+                    float *resid, const float *R, int n_slices)
+{
+    ufoir_ctx *ctx = proj->ctx;
+    const size_t n = proj->n_dets, nv = n * n;
+    proj->prm.correction_scale = -1.0f;
+    proj->prm.relaxation = lambda;
+    int rc = udev_fill(ctx->dev, x, nv * (size_t) n_slices, 0.0f);
+    if (rc)
+        return rc;
+    sart_iter it;
+    it.p = proj;
+    ufoir__projector_geom(proj, &it.g);
+    it.b = b;
+    it.x = x;
+    it.resid = resid;
+    it.R = R;
+    it.lambda = lambda;
+    it.n_slices = n_slices;
+    /* one angle sweep per graph: a sweep is already 2 * n_angles kernels */
+    int rc2 = UFOIR_OK;
+    void *exec = NULL;
+    uint64_t kernels = 0;
+    rc = udev_capture_begin(ctx->dev);
+    if (rc)
+        return rc;
+    rc = sart_body(&it);
+    rc2 = udev_capture_end(ctx->dev, &exec, &kernels);
+    if (rc || rc2) {
+        udev_graph_destroy(exec);
+        return rc ? rc : rc2;
+    }
+    for (unsigned int i = 0; i < iters && rc == UFOIR_OK; i++)
+        rc = udev_graph_launch(ctx->dev, exec, kernels);
+    if (rc == UFOIR_OK)
+        rc = udev_sync(ctx->dev);
+    udev_graph_destroy(exec);
+    return rc;
+}
+
+int ufoir_sart_process(ufoir_projector *proj, const ufoir_sart_params *prm, const float *sino,
+                       const size_t dims[2], float *vol, size_t n_slices)
+{
+    if (!proj || !prm || !sino || !vol || !dims)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc = check_relax(ctx, prm->relaxation_factor);
+    if (rc)
+        return rc;
+    rc = method_setup(proj, dims, n_slices, prm->num_iterations);
+    if (rc)
+        return rc;
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    ufoir_buf bb = {0}, bx = {0};
+    float *R = NULL, *resid = NULL;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
+    UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
+    UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices > nv ? ns * n_slices : nv));
+    proj->prm.correction_scale = 1.0f;
+    UFOIR_TRY(ray_weights(proj, R, resid));
+    UFOIR_TRY(sart_run(proj, prm->num_iterations, prm->relaxation_factor, bb.dev, bx.dev, resid, R,
+                       (int) n_slices));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
+done:
+    ufoir__free(ctx, R);
+    ufoir__free(ctx, resid);
+    ufoir__buf_release(ctx, &bb);
+    ufoir__buf_release(ctx, &bx);
+    udev_sync(ctx->dev);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ASD-POCS                                                                 */
+/* ------------------------------------------------------------------------ */
+int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
+                          const size_t dims[2], float *vol, size_t n_slices)
+{
+    if (!proj || !prm || !sino || !vol || !dims)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc;
+    if (prm->df_minimizer.num_iterations < 1)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "df_minimizer num-iterations must be >= 1");
+    if ((rc = check_relax(ctx, prm->df_minimizer.relaxation_factor)))
+        return rc;
+    if (!(prm->beta >= 0 && prm->beta_red >= 0 && prm->alpha >= 0 && prm->alpha_red >= 0 && prm->r_max >= 0))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "beta, beta_red, alpha, alpha_red, r_max must be >= 0");
+    if (prm->ng > 1000)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "ng %u outside [0, 1000]", prm->ng);
+    if (prm->norm_mode != UFOIR_NORM_COMPAT && prm->norm_mode != UFOIR_NORM_FP64)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "unknown norm_mode %d", prm->norm_mode);
+    rc = method_setup(proj, dims, n_slices, prm->num_iterations);
+    if (rc)
+        return rc;
+    const size_t n = proj->n_dets, na = proj->n_angles, nv = n * n, ns = n * na;
+    const int S = (int) n_slices;
+    udev *d = ctx->dev;
+    udev_geom g;
+    ufoir__projector_geom(proj, &g);
+    ufoir_buf bb = {0}, bo = {0};
+    float *x = NULL, *x_prev = NULL, *x_res = NULL, *b_res = NULL, *grad = NULL, *xT = NULL, *R = NULL;
+    float *dp = NULL, *dd = NULL, *dg = NULL, *dtgv = NULL, *l1 = NULL;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bo, vol, nv * n_slices, 0));
+    UFOIR_TRY(ufoir__alloc(ctx, &x, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &x_prev, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &x_res, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &b_res, ns * n_slices > nv ? ns * n_slices : nv));
+    UFOIR_TRY(ufoir__alloc(ctx, &grad, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &xT, nv * n_slices));
+    UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
+    dp = (float *) calloc((size_t) S * 5, sizeof(float));
+    if (!dp) {
+        rc = ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+        goto done;
+    }
+    dd = dp + S;
+    dg = dd + S;
+    dtgv = dg + S;
+    l1 = dtgv + S;
+    for (int s = 0; s < S; s++)
+        dp[s] = dd[s] = dg[s] = dtgv[s] = 1.0f;
+
+    UFOIR_TRY(udev_fill(d, x, nv * n_slices, 0.0f));
+    UFOIR_TRY(udev_fill(d, x_prev, nv * n_slices, 0.0f));
+    /* SART's ray weights depend on the geometry only; the reference
+     * recomputes the same values on every df_minimizer call. */
+    proj->prm.correction_scale = 1.0f;
+    UFOIR_TRY(ray_weights(proj, R, b_res));
+
+    float beta = prm->beta;
+    float sart_relax = prm->df_minimizer.relaxation_factor;
+    for (unsigned int it = 0; it < prm->num_iterations; it++) {
+        /* g_object_set(df_minimizer, "relaxation_factor", beta) (:459); the
+         * property's range is [0, 1] and GObject rejects values outside it. */
+        if (beta >= 0.0f && beta <= 1.0f)
+            sart_relax = beta;
+        UFOIR_TRY(sart_run(proj, prm->df_minimizer.num_iterations, sart_relax, bb.dev, x, b_res, R, S));
+
+        if (prm->positive_constraint)
+            UFOIR_TRY(udev_unary(d, UDEV_POSC, x, 0, 0, x, nv * n_slices));
+
+        UFOIR_TRY(udev_memcpy_async(d, bo.dev, x, nv * n_slices * sizeof(float)));
+
+        /* b_res = b - A x (:470-475) */
+        proj->prm.correction_scale = -1.0f;
+        UFOIR_TRY(udev_transpose(d, x, xT, (int) n, S));
+        UFOIR_TRY(udev_fp(d, &g, 0, (int) na, -1, x, xT, bb.dev, NULL, 0, b_res, -1.0f, S));
+        UFOIR_TRY(udev_l1_norm(d, b_res, n, na, S, prm->norm_mode, dd));
+
+        UFOIR_TRY(udev_binary(d, UDEV_SUB, x, x_prev, 0, x_res, nv * n_slices));
+        UFOIR_TRY(udev_l1_norm(d, x_res, n, n, S, prm->norm_mode, dp));
+
+        if (it == 0)
+            for (int s = 0; s < S; s++)
+                dtgv[s] = prm->alpha * dp[s];
+
+        UFOIR_TRY(udev_memcpy_async(d, x_prev, x, nv * n_slices * sizeof(float)));
+
+        /* ufo_math_tvstd_method_process_real (:550-580): 20 sub-steps */
+        for (int step = 0; step < 20; step++) {
+            UFOIR_TRY(udev_l1_grad(d, x, grad, (int) n, (int) n, S));
+            UFOIR_TRY(udev_l1_norm(d, grad, n, n, S, prm->norm_mode, l1));
+            for (int s = 0; s < S; s++) {
+                const float factor = dtgv[s] / l1[s];
+                UFOIR_TRY(udev_binary(d, UDEV_SUB_SCALED, x + (size_t) s * nv, grad + (size_t) s * nv, factor,
+                                      x + (size_t) s * nv, nv));
+            }
+        }
+
+        UFOIR_TRY(udev_binary(d, UDEV_SUB, x, x_prev, 0, x_res, nv * n_slices));
+        UFOIR_TRY(udev_l1_norm(d, x_res, n, n, S, prm->norm_mode, dg));
+        beta *= prm->beta_red;
+        for (int s = 0; s < S; s++)
+            if (dg[s] > prm->r_max * dp[s] && dd[s] > 0.001f)
+                dtgv[s] *= prm->alpha_red;
+    }
+    UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
+done:
+    free(dp);
+    ufoir__free(ctx, x);
+    ufoir__free(ctx, x_prev);
+    ufoir__free(ctx, x_res);
+    ufoir__free(ctx, b_res);
+    ufoir__free(ctx, grad);
+    ufoir__free(ctx, xT);
+    ufoir__free(ctx, R);
+    ufoir__buf_release(ctx, &bb);
+    ufoir__buf_release(ctx, &bo);
+    udev_sync(d);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Split-Bregman TV                                                         */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    ufoir_projector *p;
+    udev *d;
+    udev_geom g;
+    size_t n, nv, ns;
+    float lambda, mu;
+    int mode;
+    float *tmpA, *tmpAt, *tmpD, *tmpDxt, *inT;
+} sbtv_ctx;
+
+/* processA (sbtv-task.c:587-635): out = mu A^T A in + lambda (Dxt Dx in + Dyt Dy in). */
+static int sbtv_processA(sbtv_ctx *c, const float *in, float *out)
+{
+    udev *d = c->d;
+    const int n = (int) c->n;
+    int rc = udev_fill(d, c->tmpA, c->ns, 0.0f);
+    if (!rc)
+        rc = udev_transpose(d, in, c->inT, n, 1);
+    if (!rc)
+        rc = udev_fp(d, &c->g, 0, (int) c->p->n_angles, -1, in, c->inT, c->tmpA, NULL, 0, c->tmpA,
+                     c->p->prm.correction_scale, 1);
+    if (!rc)
+        rc = udev_bp(d, &c->g, c->p->subsets, (int) c->p->n_subsets, c->tmpA, NULL, NULL, 0, NULL, c->tmpAt,
+                     c->p->prm.relaxation, 1);
+    if (!rc)
+        rc = udev_unary(d, UDEV_SCALE, c->tmpAt, c->mu, 0, c->tmpAt, c->nv);
+    if (!rc)
+        rc = udev_diff(d, UDEV_DY, in, c->tmpD, n, n, 1);
+    if (!rc)
+        rc = udev_diff(d, UDEV_DYT, c->tmpD, out, n, n, 1);
+    if (!rc)
+        rc = udev_diff(d, UDEV_DX, in, c->tmpD, n, n, 1);
+    if (!rc)
+        rc = udev_diff(d, UDEV_DXT, c->tmpD, c->tmpDxt, n, n, 1);
+    if (!rc)
+        rc = udev_binary(d, UDEV_ADD, out, c->tmpDxt, 0, out, c->nv);
+    if (!rc)
+        rc = udev_unary(d, UDEV_SCALE, out, c->lambda, 0, out, c->nv);
+    if (!rc)
+        rc = udev_binary(d, UDEV_ADD, out, c->tmpAt, 0, out, c->nv);
+    return rc;
+}
+
+static int sbtv_dot(sbtv_ctx *c, const float *a, const float *b, float *out)
+{
+    return udev_dot(c->d, a, b, c->n, c->n, 1, c->mode, out);
+}
+
+/* l2_norm (basic-ops-processor.c:239-247): sqrt in double of the float dot. */
+static int sbtv_l2(sbtv_ctx *c, const float *a, float *out)
+{
+    float dotv = 0;
+    int rc = sbtv_dot(c, a, a, &dotv);
+    if (!rc)
+        *out = (float) sqrt((double) dotv);
+    return rc;
+}
+
+static int copy_d(sbtv_ctx *c, float *dst, const float *src)
+{
+    return udev_memcpy_async(c->d, dst, src, c->nv * sizeof(float));
+}
+
+/* cgs (sbtv-task.c:404-585). */
+static int sbtv_cgs(sbtv_ctx *c, const float *b, float *x, const float *x0, unsigned int max_iter, float **w)
+{
+    udev *d = c->d;
+    const size_t nv = c->nv;
+    float *xmin = w[0], *r = w[1], *rt = w[2], *u = w[3], *tmpa = w[4], *pp = w[5], *ph = w[6], *q = w[7];
+    float *vh = w[8], *tempSum = w[9], *uh = w[10], *qh = w[11];
+    int rc;
+    const float tol = 1E-06f;
+    float n2b;
+    if ((rc = sbtv_l2(c, b, &n2b)))
+        return rc;
+    if ((rc = copy_d(c, x, x0)))
+        return rc;
+    unsigned int flag = 1;
+    if ((rc = copy_d(c, xmin, x)))
+        return rc;
+    const float tolb = tol * n2b;
+    if ((rc = sbtv_processA(c, x, r)))
+        return rc;
+    if ((rc = udev_binary(d, UDEV_SUB, b, r, 0, r, nv)))
+        return rc;
+    float normr, normr_act;
+    if ((rc = sbtv_l2(c, r, &normr)))
+        return rc;
+    normr_act = normr;
+    if (normr <= tolb)
+        return UFOIR_OK;   /* "Initial guess is good enough" (:434-440) */
+    if ((rc = copy_d(c, rt, r)))
+        return rc;
+    float normmin = normr;
+    float rho = 1.0f;
+    unsigned int stag = 0, moresteps = 0;
+    const unsigned int maxmsteps = 5, maxstagsteps = 3;
+    if ((rc = udev_fill(d, u, nv, 0.0f)) || (rc = udev_fill(d, tmpa, nv, 0.0f)) ||
+        (rc = udev_fill(d, pp, nv, 0.0f)) || (rc = udev_fill(d, q, nv, 0.0f)) ||
+        (rc = udev_fill(d, tempSum, nv, 0.0f)))
+        return rc;
+
+    for (unsigned int iter = 0; iter < max_iter; ++iter) {
+        const float rho1 = rho;
+        if ((rc = sbtv_dot(c, rt, r, &rho)))
+            return rc;
+        if (rho == 0 || isinf(rho) || isnan(rho)) {
+            flag = 4;
+            break;
+        }
+        if (iter == 0) {
+            if ((rc = copy_d(c, u, r)) || (rc = copy_d(c, pp, u)))
+                return rc;
+        } else {
+            const float beta = rho / rho1;
+            if (beta == 0 || isinf(beta) || isnan(beta)) {
+                flag = 4;
+                break;
+            }
+            if ((rc = udev_binary(d, UDEV_ADD_SCALED, r, q, beta, u, nv)) ||
+                (rc = udev_binary(d, UDEV_ADD_SCALED, q, pp, beta, tempSum, nv)) ||
+                (rc = udev_binary(d, UDEV_ADD_SCALED, u, tempSum, beta, pp, nv)))
+                return rc;
+        }
+        if ((rc = copy_d(c, ph, pp)) || (rc = sbtv_processA(c, ph, vh)))
+            return rc;
+        float rtvh;
+        if ((rc = sbtv_dot(c, rt, vh, &rtvh)))
+            return rc;
+        float alpha = 0;
+        if (rtvh == 0) {
+            flag = 4;
+            break;
+        } else {
+            alpha = rho / rtvh;
+        }
+        if (isinf(alpha) || isnan(alpha)) {
+            flag = 4;
+            break;
+        }
+        if ((rc = udev_binary(d, UDEV_ADD_SCALED, u, vh, -alpha, q, nv)) ||
+            (rc = udev_binary(d, UDEV_ADD, u, q, 0, uh, nv)))
+            return rc;
+        float l2uh, l2x;
+        if ((rc = sbtv_l2(c, uh, &l2uh)) || (rc = sbtv_l2(c, x, &l2x)))
+            return rc;
+        /* fabs() promotes to double; EPS is the double literal 2.2204E-16 (:35, :498) */
+        if (fabs((double) alpha) * (double) l2uh < 2.2204E-16 * (double) l2x)
+            stag += 1;
+        else
+            stag = 0;
+        if ((rc = udev_binary(d, UDEV_ADD_SCALED, x, uh, alpha, x, nv)) || (rc = sbtv_processA(c, uh, qh)) ||
+            (rc = udev_binary(d, UDEV_ADD_SCALED, r, qh, -alpha, r, nv)))
+            return rc;
+        if ((rc = sbtv_l2(c, r, &normr)))
+            return rc;
+        normr_act = normr;
+        if (normr <= tolb || stag >= maxstagsteps || moresteps) {
+            /* the reference applies A to r here (:535) */
+            if ((rc = sbtv_processA(c, r, tmpa)) || (rc = udev_binary(d, UDEV_SUB, b, tmpa, 0, r, nv)) ||
+                (rc = sbtv_l2(c, r, &normr_act)))
+                return rc;
+            if (normr_act <= tolb) {
+                flag = 0;
+                break;
+            } else {
+                if (stag >= maxstagsteps && moresteps == 0)
+                    stag = 0;
+                moresteps += 1;
+                if (moresteps >= maxmsteps) {
+                    flag = 3;
+                    break;
+                }
+            }
+        }
+        if (normr_act < normmin) {
+            normmin = normr_act;
+            if ((rc = copy_d(c, xmin, x)))
+                return rc;
+        }
+        if (stag >= maxstagsteps) {
+            flag = 3;
+            break;
+        }
+    }
+    if (flag != 0) {
+        float l2r;
+        if ((rc = sbtv_processA(c, xmin, tmpa)) || (rc = udev_binary(d, UDEV_SUB, b, tmpa, 0, r, nv)) ||
+            (rc = sbtv_l2(c, r, &l2r)))
+            return rc;
+        if (l2r <= normr_act && (rc = copy_d(c, x, xmin)))
+            return rc;
+    }
+    return UFOIR_OK;
+}
+
+/* normalization (basic-ops-processor.c:342-367), in place on the device. */
+static int sbtv_normalize(udev *d, float *v, size_t count)
+{
+    float lo, hi;
+    int rc = udev_minmax(d, v, count, 1, &lo, &hi);
+    if (rc)
+        return rc;
+    const float delta = 1 / (hi - lo);
+    return udev_unary(d, UDEV_NORMALIZE, v, delta, lo, v, count);
+}
+
+#define SBTV_NBUF 26
+
+int ufoir_sbtv_process(ufoir_projector *proj, const ufoir_sbtv_params *prm, const float *sino,
+                       const size_t dims[2], float *vol, size_t n_slices)
+{
+    if (!proj || !prm || !sino || !vol || !dims)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc;
+    if (!(prm->lambda >= 0.0f) || !(prm->mu >= 0.0f))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "lambda and mu must be >= 0");
+    if (prm->norm_mode != UFOIR_NORM_COMPAT && prm->norm_mode != UFOIR_NORM_FP64)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "unknown norm_mode %d", prm->norm_mode);
+    rc = method_setup(proj, dims, n_slices, prm->num_iterations);
+    if (rc)
+        return rc;
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    udev *d = ctx->dev;
+    sbtv_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.p = proj;
+    c.d = d;
+    ufoir__projector_geom(proj, &c.g);
+    c.n = n;
+    c.nv = nv;
+    c.ns = ns;
+    c.lambda = prm->lambda;
+    c.mu = prm->mu;
+    c.mode = prm->norm_mode;
+
+    ufoir_buf bb = {0}, bo = {0};
+    float *buf[SBTV_NBUF] = {0};
+    float *f = NULL;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bo, vol, nv * n_slices, 0));
+    UFOIR_TRY(ufoir__alloc(ctx, &f, ns));
+    UFOIR_TRY(ufoir__alloc(ctx, &c.tmpA, ns));
+    for (int i = 0; i < SBTV_NBUF; i++)
+        UFOIR_TRY(ufoir__alloc(ctx, &buf[i], nv));
+    c.tmpAt = buf[12];
+    c.tmpD = buf[13];
+    c.tmpDxt = buf[14];
+    c.inT = buf[15];
+    float *fbp = buf[16], *up = buf[17], *bvec = buf[18], *bx = buf[19], *by = buf[20], *dx = buf[21];
+    float *dy = buf[22], *tmpx = buf[23], *tmpy = buf[24], *tmp = buf[25];
+
+    for (size_t s = 0; s < n_slices; s++) {
+        float *u = bo.dev + s * nv;
+        /* normalise the input (a copy; the reference does it in place, :239),
+         * copy it to f and normalise f again (:246-248) */
+        UFOIR_TRY(udev_memcpy_async(d, f, bb.dev + s * ns, ns * sizeof(float)));
+        UFOIR_TRY(sbtv_normalize(d, f, ns));
+        UFOIR_TRY(sbtv_normalize(d, f, ns));
+        /* fbp = A^T f (:251-253), u = 0, bx = by = dx = dy = 0, fbp *= mu (:279) */
+        UFOIR_TRY(udev_bp(d, &c.g, proj->subsets, (int) proj->n_subsets, f, NULL, NULL, 0, NULL, fbp,
+                          proj->prm.relaxation, 1));
+        UFOIR_TRY(udev_fill(d, u, nv, 0.0f));
+        UFOIR_TRY(udev_fill(d, bx, nv, 0.0f));
+        UFOIR_TRY(udev_fill(d, by, nv, 0.0f));
+        UFOIR_TRY(udev_fill(d, dx, nv, 0.0f));
+        UFOIR_TRY(udev_fill(d, dy, nv, 0.0f));
+        UFOIR_TRY(udev_unary(d, UDEV_SCALE, fbp, c.mu, 0, fbp, nv));
+        const float d_lambda = (float) -1 / c.lambda;
+
+        for (unsigned int it = 0; it < prm->num_iterations; ++it) {
+            UFOIR_TRY(udev_memcpy_async(d, up, u, nv * sizeof(float)));
+            /* calculate_b (:304-334) */
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, dx, bx, 0, tmp, nv));
+            UFOIR_TRY(udev_diff(d, UDEV_DXT, tmp, tmpx, (int) n, (int) n, 1));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, dy, by, 0, tmp, nv));
+            UFOIR_TRY(udev_diff(d, UDEV_DYT, tmp, tmpy, (int) n, (int) n, 1));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpx, tmpy, 0, bvec, nv));
+            UFOIR_TRY(udev_unary(d, UDEV_SCALE, bvec, c.lambda, 0, bvec, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, fbp, bvec, 0, bvec, nv));
+
+            UFOIR_TRY(sbtv_cgs(&c, bvec, u, up, 30, buf));
+
+            /* update_db (:336-402) */
+            float *s_ = buf[0], *top = buf[1], *e12 = buf[2];
+            UFOIR_TRY(udev_diff(d, UDEV_DX, u, tmpx, (int) n, (int) n, 1));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpx, bx, 0, tmpx, nv));
+            UFOIR_TRY(udev_diff(d, UDEV_DY, u, tmpy, (int) n, (int) n, 1));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpy, by, 0, tmpy, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmpx, tmpx, 0, s_, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmpy, tmpy, 0, tmp, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, s_, tmp, 0, s_, nv));
+            UFOIR_TRY(udev_unary(d, UDEV_SQRT, s_, 0, 0, s_, nv));
+            UFOIR_TRY(udev_unary(d, UDEV_ADDC, s_, d_lambda, 0, top, nv));
+            UFOIR_TRY(udev_unary(d, UDEV_MAXC, top, 0.0f, 0, top, nv));
+            UFOIR_TRY(udev_unary(d, UDEV_MAXC, s_, 1E-12f, 0, e12, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_DIV, top, e12, 0, tmp, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmp, tmpx, 0, dx, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmp, tmpy, 0, dy, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, tmpx, dx, 0, bx, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, tmpy, dy, 0, by, nv));
+        }
+    }
+    UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
+done:
+    for (int i = 0; i < SBTV_NBUF; i++)
+        ufoir__free(ctx, buf[i]);
+    ufoir__free(ctx, f);
+    ufoir__free(ctx, c.tmpA);
+    ufoir__buf_release(ctx, &bb);
+    ufoir__buf_release(ctx, &bo);
+    udev_sync(d);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Exposed reductions                                                       */
+/* ------------------------------------------------------------------------ */
+int ufoir_l1_norm(ufoir_ctx *ctx, const float *v, size_t w, size_t h, int norm_mode, float *out)
+{
+    if (!ctx || !v || !out || w == 0 || h == 0)
+        return UFOIR_ERR_INVALID;
+    ufoir_buf b = {0};
+    int rc;
+    UFOIR_TRY(ufoir__buf_in(ctx, &b, v, w * h, 1));
+    UFOIR_TRY(udev_l1_norm(ctx->dev, b.dev, w, h, 1, norm_mode, out));
+done:
+    ufoir__buf_release(ctx, &b);
+    udev_sync(ctx->dev);
+    return rc;
+}
+
+int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, size_t w, size_t h, int norm_mode,
+                      float *out)
+{
+    if (!ctx || !a || !b || !out || w == 0 || h == 0)
+        return UFOIR_ERR_INVALID;
+    ufoir_buf ba = {0}, bb = {0};
+    int rc;
+    UFOIR_TRY(ufoir__buf_in(ctx, &ba, a, w * h, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, b, w * h, 1));
+    UFOIR_TRY(udev_dot(ctx->dev, ba.dev, bb.dev, w, h, 1, norm_mode, out));
+done:
+    ufoir__buf_release(ctx, &ba);
+    ufoir__buf_release(ctx, &bb);
+    udev_sync(ctx->dev);
+    return rc;
+}

@@ -1,0 +1,436 @@
+/*
+ * projector.c - the "parallel-projector" plugin on the GPU: properties,
+ * requisition (sin/cos LUT and direction subsets), process, forward,
+ * backward and single-subset FP/BP
+ * (src/tasks/ufo-ir-parallel-projector-task.c,
+ *  src/core/ufo-ir-projector-task.c, src/core/ufo-ir-state-dependent-task.c).
+ */
+#include <ctype.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "host.h"
+
+void ufoir_projector_params_init(ufoir_projector_params *p)
+{
+    if (!p)
+        return;
+    memset(p, 0, sizeof(*p));
+    strcpy(p->model, "joseph");      /* …parallel-projector-task.c:148 */
+    p->angles_num = 0;               /* :149 */
+    p->is_forward = 1;               /* ufo-ir-state-dependent-task.c:96 */
+    p->axis_position = -1.0f;        /* ufo-ir-projector-task.c:107 */
+    p->step = 0.0f;                  /* :108 */
+    p->relaxation = 1.0f;            /* :109 */
+    p->correction_scale = 1.0f;      /* :110 */
+}
+
+static int check_params(ufoir_ctx *ctx, ufoir_projector_params *p)
+{
+    char lower[sizeof(p->model)];
+    size_t i;
+    for (i = 0; i + 1 < sizeof(lower) && p->model[i]; i++)
+        lower[i] = (char) tolower((unsigned char) p->model[i]);
+    lower[i] = 0;
+    /* set_model lower-cases the name (…parallel-projector-task.c:283-287);
+     * only projector-parallel-joseph.cl ships with the reference. */
+    if (strcmp(lower, "joseph") != 0)
+        return ufoir__fail(ctx, UFOIR_ERR_UNSUPPORTED, "projector model '%s' is not available (only 'joseph')",
+                           p->model);
+    memcpy(p->model, lower, sizeof(lower));
+    /* GParamSpec ranges (ufo-ir-projector-task.c:68-93). */
+    if (!(p->axis_position >= -1.0f))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "axis_position %g outside [-1, MAX]", (double) p->axis_position);
+    if (!(p->step >= 0.0f))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "step %g outside [0, MAX]", (double) p->step);
+    if (!isfinite(p->relaxation) || !isfinite(p->correction_scale))
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "relaxation/correction_scale must be finite");
+    return UFOIR_OK;
+}
+
+int ufoir_projector_create(ufoir_ctx *ctx, const ufoir_projector_params *p, ufoir_projector **out)
+{
+    if (!ctx || !out)
+        return UFOIR_ERR_INVALID;
+    *out = NULL;
+    ufoir_projector_params q;
+    if (p)
+        q = *p;
+    else
+        ufoir_projector_params_init(&q);
+    int rc = check_params(ctx, &q);
+    if (rc)
+        return rc;
+    ufoir_projector *proj = (ufoir_projector *) calloc(1, sizeof(*proj));
+    if (!proj)
+        return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+    proj->ctx = ctx;
+    proj->prm = q;
+    *out = proj;
+    return UFOIR_OK;
+}
+
+static void free_geometry(ufoir_projector *p)
+{
+    free(p->h_sin);
+    free(p->h_cos);
+    free(p->h_dir);
+    free(p->subsets);
+    p->h_sin = p->h_cos = NULL;
+    p->h_dir = NULL;
+    p->subsets = NULL;
+    if (p->d_sin)
+        udev_free(p->ctx->dev, p->d_sin);
+    if (p->d_cos)
+        udev_free(p->ctx->dev, p->d_cos);
+    if (p->d_dir)
+        udev_free(p->ctx->dev, p->d_dir);
+    p->d_sin = p->d_cos = NULL;
+    p->d_dir = NULL;
+    p->lut_cap = 0;
+    p->have_geometry = 0;
+}
+
+void ufoir_projector_destroy(ufoir_projector *proj)
+{
+    if (!proj)
+        return;
+    free_geometry(proj);
+    udev_sync(proj->ctx->dev);
+    free(proj);
+}
+
+int ufoir_projector_get_params(const ufoir_projector *proj, ufoir_projector_params *p)
+{
+    if (!proj || !p)
+        return UFOIR_ERR_INVALID;
+    *p = proj->prm;
+    return UFOIR_OK;
+}
+
+int ufoir_projector_set_params(ufoir_projector *proj, const ufoir_projector_params *p)
+{
+    if (!proj || !p)
+        return UFOIR_ERR_INVALID;
+    ufoir_projector_params q = *p;
+    int rc = check_params(proj->ctx, &q);
+    if (rc)
+        return rc;
+    proj->prm = q;
+    return UFOIR_OK;
+}
+
+float ufoir__axis(const ufoir_projector *p)
+{
+    /* axis_position < 0 means dims[0] / 2.0 (…parallel-projector-task.c:524-527, :584-587). */
+    float axis = p->prm.axis_position;
+    if (axis < 0)
+        axis = (float) (p->n_dets / 2.0);
+    return axis;
+}
+
+/* create_lut_buffer (…parallel-projector-task.c:437-460) and
+ * generate_full_subsets_list (:462-498). */
+static int build_geometry(ufoir_projector *p, unsigned int n_angles)
+{
+    ufoir_ctx *ctx = p->ctx;
+    const unsigned int cap = n_angles ? n_angles : 1;
+    if (cap > p->lut_cap) {
+        free_geometry(p);
+        p->h_sin = (float *) malloc(sizeof(float) * cap);
+        p->h_cos = (float *) malloc(sizeof(float) * cap);
+        p->h_dir = (unsigned char *) malloc(cap);
+        p->subsets = (ufoir_subset *) malloc(sizeof(ufoir_subset) * cap);
+        if (!p->h_sin || !p->h_cos || !p->h_dir || !p->subsets) {
+            free_geometry(p);
+            return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+        }
+        int rc = udev_malloc(ctx->dev, (void **) &p->d_sin, sizeof(float) * cap);
+        if (!rc)
+            rc = udev_malloc(ctx->dev, (void **) &p->d_cos, sizeof(float) * cap);
+        if (!rc)
+            rc = udev_malloc(ctx->dev, (void **) &p->d_dir, cap);
+        if (rc) {
+            free_geometry(p);
+            return rc;
+        }
+        p->lut_cap = cap;
+    }
+    const float step = p->prm.step;
+    for (unsigned int i = 0; i < n_angles; i++) {
+        /* guint * gfloat is a float product; sin/cos run in double. */
+        const float angle = (float) i * step;
+        p->h_sin[i] = (float) sin((double) angle);
+        p->h_cos[i] = (float) cos((double) angle);
+    }
+    unsigned int idx = 0;
+    if (n_angles > 0) {
+        int direction = fabs((double) p->h_sin[0]) <= fabs((double) p->h_cos[0]);
+        p->subsets[0].direction = direction;
+        p->subsets[0].offset = 0;
+        p->subsets[0].n = 1;
+        p->h_dir[0] = (unsigned char) direction;
+        for (unsigned int i = 1; i < n_angles; ++i) {
+            direction = fabs((double) p->h_sin[i]) <= fabs((double) p->h_cos[i]);
+            p->h_dir[i] = (unsigned char) direction;
+            if (direction != p->subsets[idx].direction) {
+                idx++;
+                p->subsets[idx].direction = direction;
+                p->subsets[idx].offset = i;
+                p->subsets[idx].n = 1;
+            } else {
+                p->subsets[idx].n++;
+            }
+        }
+        idx++;
+    }
+    p->n_subsets = idx;
+    int rc = udev_memcpy_async(ctx->dev, p->d_sin, p->h_sin, sizeof(float) * n_angles);
+    if (!rc)
+        rc = udev_memcpy_async(ctx->dev, p->d_cos, p->h_cos, sizeof(float) * n_angles);
+    if (!rc)
+        rc = udev_memcpy(ctx->dev, p->d_dir, p->h_dir, n_angles);
+    if (rc)
+        return rc;
+    p->n_angles = n_angles;
+    p->lut_step = step;
+    p->have_geometry = 1;
+    return UFOIR_OK;
+}
+
+int ufoir__projector_prepare_na(ufoir_projector *p, unsigned int n_dets, unsigned int n_angles)
+{
+    if (n_dets == 0)
+        return ufoir__fail(p->ctx, UFOIR_ERR_INVALID, "n_dets must be > 0");
+    if (n_dets > 65535)
+        return ufoir__fail(p->ctx, UFOIR_ERR_INVALID, "n_dets %u exceeds 65535", n_dets);
+    /* The reference rebuilds the LUT only when the angle count changes; a
+     * changed step is also honoured here (the reference would keep a stale LUT). */
+    if (!p->have_geometry || p->n_angles != n_angles || p->lut_step != p->prm.step) {
+        int rc = build_geometry(p, n_angles);
+        if (rc)
+            return rc;
+    }
+    p->n_dets = n_dets;
+    return UFOIR_OK;
+}
+
+int ufoir__projector_prepare(ufoir_projector *p, const size_t in_dims[2])
+{
+    if (!in_dims || in_dims[0] == 0 || in_dims[1] == 0)
+        return ufoir__fail(p->ctx, UFOIR_ERR_INVALID, "input dims must be non-zero");
+    /* angles_num == 0 takes the input's dims[1] and keeps it (:315-317). */
+    if (p->prm.angles_num == 0)
+        p->prm.angles_num = (unsigned int) in_dims[1];
+    return ufoir__projector_prepare_na(p, (unsigned int) in_dims[0], p->prm.angles_num);
+}
+
+void ufoir__projector_geom(const ufoir_projector *p, udev_geom *g)
+{
+    g->n_dets = (int) p->n_dets;
+    g->n_angles = (int) p->n_angles;
+    g->axis = ufoir__axis(p);
+    g->d_sin = p->d_sin;
+    g->d_cos = p->d_cos;
+    g->d_dir = p->d_dir;
+}
+
+int ufoir_projector_get_requisition(ufoir_projector *proj, const size_t in_dims[2], size_t out_dims[2])
+{
+    if (!proj || !in_dims || !out_dims)
+        return UFOIR_ERR_INVALID;
+    int rc = ufoir__projector_prepare(proj, in_dims);
+    if (rc)
+        return rc;
+    out_dims[0] = proj->n_dets;
+    out_dims[1] = proj->prm.is_forward ? proj->n_angles : proj->n_dets;
+    return UFOIR_OK;
+}
+
+const float *ufoir_projector_get_host_sin_vals(const ufoir_projector *proj)
+{
+    return proj && proj->have_geometry ? proj->h_sin : NULL;
+}
+
+const float *ufoir_projector_get_host_cos_vals(const ufoir_projector *proj)
+{
+    return proj && proj->have_geometry ? proj->h_cos : NULL;
+}
+
+int ufoir_projector_get_subsets(const ufoir_projector *proj, const ufoir_subset **subsets,
+                                unsigned int *count)
+{
+    if (!proj || !subsets || !count)
+        return UFOIR_ERR_INVALID;
+    if (!proj->have_geometry) {
+        *subsets = NULL;
+        *count = 0;
+        return UFOIR_ERR_STATE;
+    }
+    *subsets = proj->subsets;
+    *count = proj->n_subsets;
+    return UFOIR_OK;
+}
+
+/* Forward projection of all angles of n_slices volumes (accumulating):
+ * sino = sino + scale * A vol. Needs a transposed copy for horizontal rays. */
+static int fp_all(ufoir_projector *p, const float *dvol, float *dsino, size_t n_slices)
+{
+    ufoir_ctx *ctx = p->ctx;
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    const size_t nv = (size_t) p->n_dets * p->n_dets;
+    float *volT = NULL;
+    int rc = ufoir__alloc(ctx, &volT, nv * n_slices);
+    if (rc)
+        return rc;
+    rc = udev_transpose(ctx->dev, dvol, volT, (int) p->n_dets, (int) n_slices);
+    if (!rc)
+        rc = udev_fp(ctx->dev, &g, 0, (int) p->n_angles, -1, dvol, volT, dsino, NULL, 0, dsino,
+                     p->prm.correction_scale, (int) n_slices);
+    ufoir__free(ctx, volT);
+    return rc;
+}
+
+static int bp_all(ufoir_projector *p, float *dvol, const float *dsino, size_t n_slices)
+{
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    return udev_bp(p->ctx->dev, &g, p->subsets, (int) p->n_subsets, dsino, dvol, NULL, 0, NULL, dvol,
+                   p->prm.relaxation, (int) n_slices);
+}
+
+int ufoir_projector_forward(ufoir_projector *proj, const float *vol, float *sino, size_t n_dets,
+                            size_t n_angles, size_t n_slices)
+{
+    if (!proj || !vol || !sino || n_slices == 0)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc = ufoir__projector_prepare_na(proj, (unsigned int) n_dets, (unsigned int) n_angles);
+    if (rc)
+        return rc;
+    ufoir_buf bv = {0}, bs = {0};
+    const size_t nv = n_dets * n_dets, ns = n_dets * n_angles;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns * n_slices, 1));
+    UFOIR_TRY(fp_all(proj, bv.dev, bs.dev, n_slices));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bs, 1));
+    UFOIR_TRY(udev_sync(ctx->dev));
+done:
+    ufoir__buf_release(ctx, &bv);
+    ufoir__buf_release(ctx, &bs);
+    return rc;
+}
+
+int ufoir_projector_backward(ufoir_projector *proj, float *vol, const float *sino, size_t n_dets,
+                             size_t n_angles, size_t n_slices)
+{
+    if (!proj || !vol || !sino || n_slices == 0)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc = ufoir__projector_prepare_na(proj, (unsigned int) n_dets, (unsigned int) n_angles);
+    if (rc)
+        return rc;
+    ufoir_buf bv = {0}, bs = {0};
+    const size_t nv = n_dets * n_dets, ns = n_dets * n_angles;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns * n_slices, 1));
+    UFOIR_TRY(bp_all(proj, bv.dev, bs.dev, n_slices));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bv, 1));
+    UFOIR_TRY(udev_sync(ctx->dev));
+done:
+    ufoir__buf_release(ctx, &bv);
+    ufoir__buf_release(ctx, &bs);
+    return rc;
+}
+
+int ufoir_projector_process(ufoir_projector *proj, const float *in, const size_t in_dims[2], float *out,
+                            size_t n_slices)
+{
+    if (!proj || !in || !out || !in_dims || n_slices == 0)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    size_t out_dims[2];
+    int rc = ufoir_projector_get_requisition(proj, in_dims, out_dims);
+    if (rc)
+        return rc;
+    const size_t n = proj->n_dets;
+    const size_t nv = n * n, ns = n * proj->n_angles;
+    ufoir_buf bi = {0}, bo = {0};
+    if (proj->prm.is_forward) {
+        /* input is a volume n x n (its dims[1] must match) */
+        if (in_dims[1] != n)
+            return ufoir__fail(ctx, UFOIR_ERR_INVALID, "forward input must be %zu x %zu", n, n);
+        UFOIR_TRY(ufoir__buf_in(ctx, &bi, in, nv * n_slices, 1));
+        UFOIR_TRY(ufoir__buf_in(ctx, &bo, out, ns * n_slices, 0));
+        UFOIR_TRY(udev_fill(ctx->dev, bo.dev, ns * n_slices, 0.0f));
+        UFOIR_TRY(fp_all(proj, bi.dev, bo.dev, n_slices));
+    } else {
+        if (in_dims[1] != proj->n_angles)
+            return ufoir__fail(ctx, UFOIR_ERR_INVALID, "angles_num %u does not match the sinogram's %zu rows",
+                               proj->n_angles, in_dims[1]);
+        UFOIR_TRY(ufoir__buf_in(ctx, &bi, in, ns * n_slices, 1));
+        UFOIR_TRY(ufoir__buf_in(ctx, &bo, out, nv * n_slices, 0));
+        UFOIR_TRY(udev_fill(ctx->dev, bo.dev, nv * n_slices, 0.0f));
+        UFOIR_TRY(bp_all(proj, bo.dev, bi.dev, n_slices));
+    }
+    UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
+    UFOIR_TRY(udev_sync(ctx->dev));
+done:
+    ufoir__buf_release(ctx, &bi);
+    ufoir__buf_release(ctx, &bo);
+    return rc;
+}
+
+int ufoir_projector_subset_fp(ufoir_projector *proj, const float *vol, float *sino, const ufoir_subset *s)
+{
+    if (!proj || !vol || !sino || !s)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    if (!proj->have_geometry)
+        return ufoir__fail(ctx, UFOIR_ERR_STATE, "subset_fp before the geometry is known (no requisition yet)");
+    if (s->offset + (size_t) s->n > proj->n_angles)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "subset outside the %u angles", proj->n_angles);
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    ufoir_buf bv = {0}, bs = {0};
+    udev_geom g;
+    ufoir__projector_geom(proj, &g);
+    int rc;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns, 1));
+    /* The subset's own direction picks the kernel (…parallel-projector-task.c:570). */
+    UFOIR_TRY(udev_fp(ctx->dev, &g, (int) s->offset, (int) s->n, s->direction ? 1 : 0, bv.dev, NULL, bs.dev,
+                      NULL, 0, bs.dev, proj->prm.correction_scale, 1));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bs, 1));
+    UFOIR_TRY(udev_sync(ctx->dev));
+done:
+    ufoir__buf_release(ctx, &bv);
+    ufoir__buf_release(ctx, &bs);
+    return rc;
+}
+
+int ufoir_projector_subset_bp(ufoir_projector *proj, float *vol, const float *sino, const ufoir_subset *s)
+{
+    if (!proj || !vol || !sino || !s)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    if (!proj->have_geometry)
+        return ufoir__fail(ctx, UFOIR_ERR_STATE, "subset_bp before the geometry is known (no requisition yet)");
+    if (s->offset + (size_t) s->n > proj->n_angles)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "subset outside the %u angles", proj->n_angles);
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    ufoir_buf bv = {0}, bs = {0};
+    udev_geom g;
+    ufoir__projector_geom(proj, &g);
+    int rc;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns, 1));
+    UFOIR_TRY(udev_bp(ctx->dev, &g, s, 1, bs.dev, bv.dev, NULL, 0, NULL, bv.dev, proj->prm.relaxation, 1));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bv, 1));
+    UFOIR_TRY(udev_sync(ctx->dev));
+done:
+    ufoir__buf_release(ctx, &bv);
+    ufoir__buf_release(ctx, &bs);
+    return rc;
+}

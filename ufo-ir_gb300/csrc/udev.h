@@ -1,0 +1,130 @@
+/*
+ * udev.h - thin C ABI between the C host library and the CUDA layer.
+ *
+ * The host code (geometry, projector, methods, serve loop; all C) never
+ * includes CUDA headers: it allocates, copies, launches and captures graphs
+ * through these functions, implemented in the .cu files of this directory.
+ * Every function returns 0 or a negative ufoir_status and records a message
+ * retrievable with udev_error().
+ */
+#ifndef UFOIR_UDEV_H
+#define UFOIR_UDEV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "ufoir.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct udev udev;
+
+int udev_create(int device, udev **out, char *err, size_t errlen);
+void udev_destroy(udev *d);
+const char *udev_error(const udev *d);
+void udev_set_error(udev *d, const char *fmt, ...);
+int udev_device(const udev *d);
+int udev_sync(udev *d);
+void *udev_stream(udev *d);
+uint64_t udev_launches(const udev *d);
+int udev_mem_info(udev *d, size_t *free_bytes, size_t *total_bytes);
+int udev_sm_count(const udev *d);
+
+int udev_malloc(udev *d, void **p, size_t bytes);           /* stream-ordered */
+int udev_free(udev *d, void *p);
+int udev_host_malloc(udev *d, void **p, size_t bytes);      /* page-locked */
+int udev_host_free(udev *d, void *p);
+/* 1 if p is device memory of this context's GPU, 0 if host memory. */
+int udev_is_device_ptr(udev *d, const void *p);
+int udev_memcpy_async(udev *d, void *dst, const void *src, size_t bytes);
+int udev_memcpy(udev *d, void *dst, const void *src, size_t bytes);   /* + stream sync */
+
+/* ---- Device-side projection geometry (built by the host from the LUT). ---- */
+typedef struct {
+    int n_dets;                    /* detector count = volume side */
+    int n_angles;
+    float axis;                    /* resolved axis position */
+    const float *d_sin;            /* [n_angles] float LUT */
+    const float *d_cos;
+    const unsigned char *d_dir;    /* [n_angles] direction of each angle (full subsets) */
+} udev_geom;
+
+/* Forward projection of angles [a0, a0 + na) for n_slices slices:
+ *   out = (src + scale * S) [* w]        (S = Joseph ray sum, 64-sample blocks)
+ * Inactive detectors (axis off-centre) give out = src [* w].
+ * dir_override < 0 uses the per-angle direction, else forces it.
+ * vol is [n][n] per slice; volT its transpose, read by horizontal rays (if
+ * NULL they read vol column-wise instead). src/out/w are full sinograms
+ * [n_angles][n] per slice; src may equal out; w may be NULL; w_shared != 0
+ * means one w for all slices. */
+int udev_fp(udev *d, const udev_geom *g, int a0, int na, int dir_override,
+            const float *vol, const float *volT, const float *src, const float *w,
+            int w_shared, float *out, float scale, int n_slices);
+
+/* Transpose n x n slices. */
+int udev_transpose(udev *d, const float *in, float *out, int n, int n_slices);
+
+/* Pixel-driven backprojection over a list of subsets:
+ *   v = base ? base : 0;  for each subset: v = v + relax * sum_{angles} lerp(sino)
+ *   if cw: v = v * cw;  if add: v = v + add;  dst = v
+ * base / add may alias dst; cw_shared != 0 means one cw for all slices. */
+int udev_bp(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
+            const float *sino, const float *base, const float *cw, int cw_shared,
+            const float *add, float *dst, float relax, int n_slices);
+
+/* ---- Element-wise ops over n contiguous floats. ---- */
+enum {
+    UDEV_MUL = 0,        /* a * b */
+    UDEV_ADD = 1,        /* a + b */
+    UDEV_SUB = 2,        /* a - b */
+    UDEV_SUB_SCALED = 3, /* a - m * b */
+    UDEV_ADD_SCALED = 4, /* a + m * b */
+    UDEV_MAX = 5,        /* fmax(a, b) */
+    UDEV_DIV = 6         /* a / b */
+};
+enum {
+    UDEV_INV = 0,        /* a != 0 ? 1 / a : 0 */
+    UDEV_POSC = 1,       /* a > 0 ? a : 0 */
+    UDEV_SQRT = 2,       /* sqrt(a) correctly rounded */
+    UDEV_SCALE = 3,      /* a * m */
+    UDEV_ADDC = 4,       /* m + a */
+    UDEV_MAXC = 5,       /* fmax(a, m) */
+    UDEV_NORMALIZE = 6   /* delta * a - lo * delta; m = delta, m2 = lo */
+};
+int udev_fill(udev *d, float *p, size_t n, float v);
+int udev_binary(udev *d, int op, const float *a, const float *b, float m, float *out, size_t n);
+int udev_unary(udev *d, int op, const float *a, float m, float m2, float *out, size_t n);
+
+/* TV subgradient (l1_grad) of n_slices w x h images. */
+int udev_l1_grad(udev *d, const float *in, float *out, int w, int h, int n_slices);
+/* Periodic differences. */
+enum { UDEV_DX = 0, UDEV_DXT = 1, UDEV_DY = 2, UDEV_DYT = 3 };
+int udev_diff(udev *d, int which, const float *in, float *out, int w, int h, int n_slices);
+
+/* ---- Reductions; one float per slice written to host memory. ---- */
+/* sum |v| over each w*h slice, in the index order of ufo_ir_op_l1_norm. */
+int udev_l1_norm(udev *d, const float *v, size_t w, size_t h, int n_slices, int mode,
+                 float *host_out);
+/* buggy-index dot product of ufo_ir_basic_ops_processor_dot_product. */
+int udev_dot(udev *d, const float *a, const float *b, size_t w, size_t h, int n_slices,
+             int mode, float *host_out);
+/* min and max of each slice (exact; order independent). */
+int udev_minmax(udev *d, const float *v, size_t n, int n_slices, float *host_min, float *host_max);
+
+/* ---- Timing with CUDA events on the context's stream ---- */
+int udev_timer_begin(udev *d);
+int udev_timer_end(udev *d, float *ms);   /* waits for the stop event */
+
+/* ---- CUDA graphs ---- */
+int udev_capture_begin(udev *d);
+/* Ends the capture and instantiates it. *kernels = kernel launches captured. */
+int udev_capture_end(udev *d, void **exec, uint64_t *kernels);
+int udev_graph_launch(udev *d, void *exec, uint64_t kernels);
+void udev_graph_destroy(void *exec);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,328 @@
+/*
+ * udev_runtime.cu - context, memory, copies and CUDA-graph capture for the
+ * C host library (declared in udev.h).
+ */
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "udev_internal.cuh"
+
+extern "C" {
+
+void udev_set_error(udev *d, const char *fmt, ...)
+{
+    if (!d)
+        return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(d->err, sizeof(d->err), fmt, ap);
+    va_end(ap);
+}
+
+const char *udev_error(const udev *d)
+{
+    return d ? d->err : "no context";
+}
+
+int udev_create(int device, udev **out, char *err, size_t errlen)
+{
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        snprintf(err, errlen, "no CUDA device available (%s)",
+                 e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        cudaGetLastError();
+        return UFOIR_ERR_CUDA;
+    }
+    if (device < 0 || device >= count) {
+        snprintf(err, errlen, "device %d out of range [0, %d)", device, count);
+        return UFOIR_ERR_INVALID;
+    }
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        snprintf(err, errlen, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
+    }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) {
+        snprintf(err, errlen, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
+    }
+    if (prop.major < 10) {
+        snprintf(err, errlen, "device %d is sm_%d%d; this library is built for sm_103a only",
+                 device, prop.major, prop.minor);
+        return UFOIR_ERR_UNSUPPORTED;
+    }
+    udev *d = new (std::nothrow) udev();
+    if (!d) {
+        snprintf(err, errlen, "out of host memory");
+        return UFOIR_ERR_NOMEM;
+    }
+    d->device = device;
+    d->sm_count = prop.multiProcessorCount;
+    d->smem_optin = (int) prop.sharedMemPerBlockOptin;
+    e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        snprintf(err, errlen, "cudaStreamCreate: %s", cudaGetErrorString(e));
+        delete d;
+        return UFOIR_ERR_CUDA;
+    }
+    /* Keep freed stream-ordered memory in the pool instead of returning it to
+     * the driver after every synchronisation. */
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    cudaGetLastError();
+    *out = d;
+    return UFOIR_OK;
+}
+
+void udev_destroy(udev *d)
+{
+    if (!d)
+        return;
+    cudaSetDevice(d->device);
+    cudaStreamSynchronize(d->stream);
+    if (d->red_partials)
+        cudaFree(d->red_partials);
+    if (d->red_out)
+        cudaFree(d->red_out);
+    if (d->h_red)
+        cudaFreeHost(d->h_red);
+    if (d->ev_start)
+        cudaEventDestroy(d->ev_start);
+    if (d->ev_stop)
+        cudaEventDestroy(d->ev_stop);
+    cudaStreamDestroy(d->stream);
+    delete d;
+}
+
+int udev_device(const udev *d)
+{
+    return d->device;
+}
+
+int udev_sm_count(const udev *d)
+{
+    return d->sm_count;
+}
+
+void *udev_stream(udev *d)
+{
+    return (void *) d->stream;
+}
+
+uint64_t udev_launches(const udev *d)
+{
+    return d->launches;
+}
+
+int udev_sync(udev *d)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaStreamSynchronize(d->stream));
+    return UFOIR_OK;
+}
+
+int udev_mem_info(udev *d, size_t *free_bytes, size_t *total_bytes)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaMemGetInfo(free_bytes, total_bytes));
+    return UFOIR_OK;
+}
+
+int udev_malloc(udev *d, void **p, size_t bytes)
+{
+    UDEV_BIND(d);
+    *p = nullptr;
+    if (bytes == 0)
+        bytes = 16;
+    cudaError_t e = cudaMallocAsync(p, bytes, d->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        udev_set_error(d, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? UFOIR_ERR_NOMEM : UFOIR_ERR_CUDA;
+    }
+    return UFOIR_OK;
+}
+
+int udev_free(udev *d, void *p)
+{
+    if (!p)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaFreeAsync(p, d->stream));
+    return UFOIR_OK;
+}
+
+int udev_host_malloc(udev *d, void **p, size_t bytes)
+{
+    UDEV_BIND(d);
+    *p = nullptr;
+    cudaError_t e = cudaMallocHost(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        udev_set_error(d, "pinned host allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return UFOIR_ERR_NOMEM;
+    }
+    return UFOIR_OK;
+}
+
+int udev_host_free(udev *d, void *p)
+{
+    if (!p)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaFreeHost(p));
+    return UFOIR_OK;
+}
+
+int udev_is_device_ptr(udev *d, const void *p)
+{
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)
+        return attr.device == d->device ? 1 : 0;
+    return 0;
+}
+
+int udev_memcpy_async(udev *d, void *dst, const void *src, size_t bytes)
+{
+    if (bytes == 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, d->stream));
+    return UFOIR_OK;
+}
+
+int udev_memcpy(udev *d, void *dst, const void *src, size_t bytes)
+{
+    int rc = udev_memcpy_async(d, dst, src, bytes);
+    if (rc)
+        return rc;
+    return udev_sync(d);
+}
+
+int udev_timer_begin(udev *d)
+{
+    UDEV_BIND(d);
+    if (!d->ev_start) {
+        UDEV_CHECK(d, cudaEventCreate(&d->ev_start));
+        UDEV_CHECK(d, cudaEventCreate(&d->ev_stop));
+    }
+    UDEV_CHECK(d, cudaEventRecord(d->ev_start, d->stream));
+    return UFOIR_OK;
+}
+
+int udev_timer_end(udev *d, float *ms)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaEventRecord(d->ev_stop, d->stream));
+    UDEV_CHECK(d, cudaEventSynchronize(d->ev_stop));
+    UDEV_CHECK(d, cudaEventElapsedTime(ms, d->ev_start, d->ev_stop));
+    return UFOIR_OK;
+}
+
+int udev_capture_begin(udev *d)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+    d->capturing = 1;
+    d->capture_launches = 0;
+    return UFOIR_OK;
+}
+
+int udev_capture_end(udev *d, void **exec, uint64_t *kernels)
+{
+    UDEV_BIND(d);
+    cudaGraph_t graph = nullptr;
+    d->capturing = 0;
+    *exec = nullptr;
+    cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        udev_set_error(d, "graph capture failed: %s", cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
+    }
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        udev_set_error(d, "graph instantiate failed: %s", cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
+    }
+    *exec = (void *) ge;
+    if (kernels)
+        *kernels = d->capture_launches;
+    return UFOIR_OK;
+}
+
+int udev_graph_launch(udev *d, void *exec, uint64_t kernels)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaGraphLaunch((cudaGraphExec_t) exec, d->stream));
+    d->launches += kernels;
+    return UFOIR_OK;
+}
+
+void udev_graph_destroy(void *exec)
+{
+    if (exec)
+        cudaGraphExecDestroy((cudaGraphExec_t) exec);
+}
+
+}  /* extern "C" */
+
+int udev_after_launch(udev *d, const char *what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        udev_set_error(d, "launch of %s failed: %s", what, cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
+    }
+    if (d->capturing)
+        d->capture_launches++;
+    else
+        d->launches++;
+    return UFOIR_OK;
+}
+
+int udev_reduction_scratch(udev *d, size_t partials, size_t outs)
+{
+    if (partials > d->red_partials_cap) {
+        if (d->red_partials)
+            cudaFree(d->red_partials);
+        d->red_partials = nullptr;
+        d->red_partials_cap = 0;
+        UDEV_CHECK(d, cudaMalloc(&d->red_partials, partials * sizeof(double)));
+        d->red_partials_cap = partials;
+    }
+    if (outs > d->red_out_cap) {
+        if (d->red_out)
+            cudaFree(d->red_out);
+        if (d->h_red)
+            cudaFreeHost(d->h_red);
+        d->red_out = nullptr;
+        d->h_red = nullptr;
+        d->red_out_cap = 0;
+        UDEV_CHECK(d, cudaMalloc(&d->red_out, 2 * outs * sizeof(float)));
+        UDEV_CHECK(d, cudaMallocHost(&d->h_red, 2 * outs * sizeof(float)));
+        d->red_out_cap = outs;
+    }
+    return UFOIR_OK;
+}
