@@ -113,8 +113,15 @@ def test_sbtv_matches_oracle(ufoir_lib, gpu_ctx, oracle, mode):
     assert rel_l2(got, want) <= TOL_ITER
     if mode == "compat":
         assert np.array_equal(got, want), np.abs(got - want).max()
+    # Error against the FP64 recomputation, stated rather than bounded tightly:
+    # the reference's CGS (with its partNum * i inner product) follows a
+    # different trajectory in double precision; the float and double results
+    # of the reference algorithm itself differ by about 6 % after 2 outer
+    # iterations here (9e-4 after 1).
     wd = oracle.sbtv_d(oracle.projector(n, na, step), sino, prm)
-    assert rel_l2(got, wd) < 1e-3
+    err64 = rel_l2(got, wd)
+    print(f"sbtv {mode}: rel-L2 vs FP64 recomputation {err64:.3e}")
+    assert err64 < 0.1
 
 
 def test_norms_match_oracle(ufoir_lib, gpu_ctx, oracle):

@@ -175,6 +175,18 @@ def test_full_size_geometry_properties(ufoir_lib, gpu_ctx):
     sino.close()
 
 
+def test_row_kernel_serves_sizes_beyond_the_tiled_kernel(ufoir_lib, gpu_ctx):
+    # n = 6200 needs more than 768 threads x 8 detectors: the row kernel
+    # (one thread per ray, no shared memory) projects it instead.
+    n, na = 6200, 4
+    p = _proj(ufoir_lib, gpu_ctx, n, na, np.float32(np.pi / na))
+    ones = ufoir_lib.DeviceArray.from_numpy(gpu_ctx, np.ones((n, n), np.float32))
+    sino = p.forward(ones, np.zeros((na, n), np.float32))
+    assert np.all(sino[0] == n)
+    assert np.isfinite(sino).all() and sino[2].max() == n   # theta = pi/2: horizontal rays
+    ones.close()
+
+
 def test_full_size_bp_matches_oracle_on_a_row_band(ufoir_lib, gpu_ctx, oracle):
     # C1 geometry in full (367 bins, 180 angles), compared with the oracle.
     n, na = 367, 180

@@ -168,8 +168,9 @@ int ufoir__buf_in(ufoir_ctx *ctx, ufoir_buf *b, const float *user, size_t count,
 
 int ufoir__buf_out(ufoir_ctx *ctx, ufoir_buf *b, int copy_out)
 {
-    int rc = UFOIR_OK;
-    if (b->owned && copy_out)
+    /* a kernel that gave up on a bounded wait invalidates the result */
+    int rc = udev_take_kernel_error(ctx->dev);
+    if (rc == UFOIR_OK && b->owned && copy_out)
         rc = udev_memcpy(ctx->dev, b->user, b->dev, b->count * sizeof(float));
     ufoir__buf_release(ctx, b);
     return rc;

@@ -31,7 +31,29 @@ struct ufoir_projector {
     float *d_sin, *d_cos;
     unsigned char *d_dir;
     unsigned int lut_cap;
+    /* angle tiles of the tiled forward projector (int4 each, device) */
+    void *d_tiles;
+    int n_tiles;
+    int tiles_A;
+    int tiles_valid;
 };
+
+/* Scratch of the tiled forward projector: the padded copy and the padded
+ * transpose of n_slices volumes (pad columns zero). */
+typedef struct {
+    float *P, *TP;
+    size_t slices;
+} ufoir_fp_scratch;
+
+int ufoir__fp_scratch_alloc(ufoir_projector *p, ufoir_fp_scratch *s, size_t slices);
+void ufoir__fp_scratch_free(ufoir_projector *p, ufoir_fp_scratch *s);
+/* Forward projection of all angles: out = (src + scale * A vol) [* w]. */
+int ufoir__fp_full(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, const float *src, const float *w,
+                   int w_shared, float *out, float scale, int n_slices);
+/* The two launches of ufoir__fp_full, separately (for timing). */
+int ufoir__fp_prepare(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, int n_slices);
+int ufoir__fp_project(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, const float *src, const float *w,
+                      int w_shared, float *out, float scale, int n_slices);
 
 /* Error helpers: record a message on the context and return the status. */
 int ufoir__fail(ufoir_ctx *ctx, int status, const char *fmt, ...);

@@ -94,17 +94,19 @@ static int check_relax(ufoir_ctx *ctx, float r)
 static int ray_weights(ufoir_projector *p, float *R, float *ones)
 {
     ufoir_ctx *ctx = p->ctx;
-    udev_geom g;
-    ufoir__projector_geom(p, &g);
     const size_t n = p->n_dets, nv = n * n, ns = n * p->n_angles;
-    int rc = udev_fill(ctx->dev, ones, nv, 1.0f);
+    ufoir_fp_scratch fs;
+    int rc = ufoir__fp_scratch_alloc(p, &fs, 1);
+    if (rc)
+        return rc;
+    rc = udev_fill(ctx->dev, ones, nv, 1.0f);
     if (!rc)
         rc = udev_fill(ctx->dev, R, ns, 0.0f);
-    /* the transpose of a constant image is itself */
     if (!rc)
-        rc = udev_fp(ctx->dev, &g, 0, (int) p->n_angles, -1, ones, ones, R, NULL, 0, R, 1.0f, 1);
+        rc = ufoir__fp_full(p, &fs, ones, R, NULL, 0, R, 1.0f, 1);
     if (!rc)
         rc = udev_unary(ctx->dev, UDEV_INV, R, 0, 0, R, ns);
+    ufoir__fp_scratch_free(p, &fs);
     return rc;
 }
 
@@ -170,7 +172,8 @@ typedef struct {
     ufoir_projector *p;
     udev_geom g;
     const float *b;
-    float *x, *xT, *resid;
+    float *x, *resid;
+    ufoir_fp_scratch fs;
     const float *R, *C;
     float lambda;
     int n_slices;
@@ -180,12 +183,8 @@ static int sirt_body(void *arg)
 {
     sirt_iter *s = (sirt_iter *) arg;
     udev *d = s->p->ctx->dev;
-    const int n = (int) s->p->n_dets;
     /* sirt-task.c:202-213: r = (b - A x) * R;  x = x + C * (lambda A^T r) */
-    int rc = udev_transpose(d, s->x, s->xT, n, s->n_slices);
-    if (!rc)
-        rc = udev_fp(d, &s->g, 0, (int) s->p->n_angles, -1, s->x, s->xT, s->b, s->R, 1, s->resid, -1.0f,
-                     s->n_slices);
+    int rc = ufoir__fp_full(s->p, &s->fs, s->x, s->b, s->R, 1, s->resid, -1.0f, s->n_slices);
     if (!rc)
         rc = udev_bp(d, &s->g, s->p->subsets, (int) s->p->n_subsets, s->resid, NULL, s->C, 1, s->x, s->x,
                      s->lambda, s->n_slices);
@@ -206,40 +205,42 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
         return rc;
     const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
     ufoir_buf bb = {0}, bx = {0};
-    float *R = NULL, *C = NULL, *xT = NULL, *resid = NULL;
+    float *R = NULL, *C = NULL, *resid = NULL;
+    sirt_iter it;
+    memset(&it, 0, sizeof(it));
     UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
     UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &C, nv));
-    UFOIR_TRY(ufoir__alloc(ctx, &xT, nv * n_slices));
     UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices));
+    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &it.fs, n_slices));
 
-    /* weights with relaxation 1 and correction scale 1 (sirt-task.c:176-193) */
+    /* weights with relaxation 1 and correction scale 1 (sirt-task.c:176-193);
+     * the output volume serves as the all-ones image before it is zeroed */
     proj->prm.relaxation = 1.0f;
     proj->prm.correction_scale = 1.0f;
-    UFOIR_TRY(ray_weights(proj, R, xT));
+    UFOIR_TRY(ray_weights(proj, R, bx.dev));
     UFOIR_TRY(pixel_weights(proj, C, resid));
     proj->prm.relaxation = prm->relaxation_factor;
     proj->prm.correction_scale = -1.0f;
     UFOIR_TRY(udev_fill(ctx->dev, bx.dev, nv * n_slices, 0.0f));
 
-    sirt_iter it;
     it.p = proj;
     ufoir__projector_geom(proj, &it.g);
     it.b = bb.dev;
     it.x = bx.dev;
-    it.xT = xT;
     it.resid = resid;
     it.R = R;
     it.C = C;
     it.lambda = prm->relaxation_factor;
     it.n_slices = (int) n_slices;
     UFOIR_TRY(run_graphed(ctx, prm->num_iterations, sirt_body, &it));
+    UFOIR_TRY(udev_take_kernel_error(ctx->dev));
     UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
 done:
     ufoir__free(ctx, R);
     ufoir__free(ctx, C);
-    ufoir__free(ctx, xT);
+    ufoir__fp_scratch_free(proj, &it.fs);
     ufoir__free(ctx, resid);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bx);
@@ -256,7 +257,7 @@ done:
 struct ufoir_sirt_batch {
     ufoir_projector *proj;
     sirt_iter it;
-    float *R, *C, *xT, *resid;
+    float *R, *C, *resid;
     size_t nv;
     void *exec;
     uint64_t exec_kernels;
@@ -271,8 +272,8 @@ void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b)
     udev_graph_destroy(b->exec);
     ufoir__free(ctx, b->R);
     ufoir__free(ctx, b->C);
-    ufoir__free(ctx, b->xT);
     ufoir__free(ctx, b->resid);
+    ufoir__fp_scratch_free(b->proj, &b->it.fs);
     udev_sync(ctx->dev);
     free(b);
 }
@@ -300,11 +301,11 @@ int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *prm,
     b->nv = nv;
     UFOIR_TRY(ufoir__alloc(ctx, &b->R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &b->C, nv));
-    UFOIR_TRY(ufoir__alloc(ctx, &b->xT, nv * n_slices));
     UFOIR_TRY(ufoir__alloc(ctx, &b->resid, ns * n_slices));
+    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &b->it.fs, n_slices));
     proj->prm.relaxation = 1.0f;
     proj->prm.correction_scale = 1.0f;
-    UFOIR_TRY(ray_weights(proj, b->R, b->xT));
+    UFOIR_TRY(ray_weights(proj, b->R, d_vol));
     UFOIR_TRY(pixel_weights(proj, b->C, b->resid));
     proj->prm.relaxation = prm->relaxation_factor;
     proj->prm.correction_scale = -1.0f;
@@ -313,7 +314,6 @@ int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *prm,
     ufoir__projector_geom(proj, &b->it.g);
     b->it.b = d_sino;
     b->it.x = d_vol;
-    b->it.xT = b->xT;
     b->it.resid = b->resid;
     b->it.R = b->R;
     b->it.C = b->C;
@@ -346,7 +346,7 @@ int ufoir_sirt_batch_run(ufoir_sirt_batch *b, unsigned int iterations)
         if (rc)
             return rc;
     }
-    return udev_sync(d);
+    return udev_take_kernel_error(d);
 }
 
 int ufoir_sirt_batch_reset(ufoir_sirt_batch *b)
@@ -364,14 +364,12 @@ int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3])
         return UFOIR_ERR_INVALID;
     sirt_iter *s = &b->it;
     udev *d = s->p->ctx->dev;
-    const int n = (int) s->p->n_dets;
     int rc;
-    if ((rc = udev_timer_begin(d)) || (rc = udev_transpose(d, s->x, s->xT, n, s->n_slices)) ||
+    if ((rc = udev_timer_begin(d)) || (rc = ufoir__fp_prepare(s->p, &s->fs, s->x, s->n_slices)) ||
         (rc = udev_timer_end(d, &ms[0])))
         return rc;
     if ((rc = udev_timer_begin(d)) ||
-        (rc = udev_fp(d, &s->g, 0, (int) s->p->n_angles, -1, s->x, s->xT, s->b, s->R, 1, s->resid, -1.0f,
-                      s->n_slices)) ||
+        (rc = ufoir__fp_project(s->p, &s->fs, s->x, s->b, s->R, 1, s->resid, -1.0f, s->n_slices)) ||
         (rc = udev_timer_end(d, &ms[1])))
         return rc;
     if ((rc = udev_timer_begin(d)) ||
@@ -379,7 +377,7 @@ int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3])
                       s->lambda, s->n_slices)) ||
         (rc = udev_timer_end(d, &ms[2])))
         return rc;
-    return UFOIR_OK;
+    return udev_take_kernel_error(d);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -518,7 +516,8 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
     udev_geom g;
     ufoir__projector_geom(proj, &g);
     ufoir_buf bb = {0}, bo = {0};
-    float *x = NULL, *x_prev = NULL, *x_res = NULL, *b_res = NULL, *grad = NULL, *xT = NULL, *R = NULL;
+    float *x = NULL, *x_prev = NULL, *x_res = NULL, *b_res = NULL, *grad = NULL, *R = NULL;
+    ufoir_fp_scratch fs = {NULL, NULL, 0};
     float *dp = NULL, *dd = NULL, *dg = NULL, *dtgv = NULL, *l1 = NULL;
     UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bo, vol, nv * n_slices, 0));
@@ -527,7 +526,7 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
     UFOIR_TRY(ufoir__alloc(ctx, &x_res, nv * n_slices));
     UFOIR_TRY(ufoir__alloc(ctx, &b_res, ns * n_slices > nv ? ns * n_slices : nv));
     UFOIR_TRY(ufoir__alloc(ctx, &grad, nv * n_slices));
-    UFOIR_TRY(ufoir__alloc(ctx, &xT, nv * n_slices));
+    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &fs, n_slices));
     UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
     dp = (float *) calloc((size_t) S * 5, sizeof(float));
     if (!dp) {
@@ -564,8 +563,7 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
 
         /* b_res = b - A x (:470-475) */
         proj->prm.correction_scale = -1.0f;
-        UFOIR_TRY(udev_transpose(d, x, xT, (int) n, S));
-        UFOIR_TRY(udev_fp(d, &g, 0, (int) na, -1, x, xT, bb.dev, NULL, 0, b_res, -1.0f, S));
+        UFOIR_TRY(ufoir__fp_full(proj, &fs, x, bb.dev, NULL, 0, b_res, -1.0f, S));
         UFOIR_TRY(udev_l1_norm(d, b_res, n, na, S, prm->norm_mode, dd));
 
         UFOIR_TRY(udev_binary(d, UDEV_SUB, x, x_prev, 0, x_res, nv * n_slices));
@@ -603,7 +601,7 @@ done:
     ufoir__free(ctx, x_res);
     ufoir__free(ctx, b_res);
     ufoir__free(ctx, grad);
-    ufoir__free(ctx, xT);
+    ufoir__fp_scratch_free(proj, &fs);
     ufoir__free(ctx, R);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bo);
@@ -621,7 +619,8 @@ typedef struct {
     size_t n, nv, ns;
     float lambda, mu;
     int mode;
-    float *tmpA, *tmpAt, *tmpD, *tmpDxt, *inT;
+    float *tmpA, *tmpAt, *tmpD, *tmpDxt;
+    ufoir_fp_scratch fs;
 } sbtv_ctx;
 
 /* processA (sbtv-task.c:587-635): out = mu A^T A in + lambda (Dxt Dx in + Dyt Dy in). */
@@ -631,10 +630,7 @@ static int sbtv_processA(sbtv_ctx *c, const float *in, float *out)
     const int n = (int) c->n;
     int rc = udev_fill(d, c->tmpA, c->ns, 0.0f);
     if (!rc)
-        rc = udev_transpose(d, in, c->inT, n, 1);
-    if (!rc)
-        rc = udev_fp(d, &c->g, 0, (int) c->p->n_angles, -1, in, c->inT, c->tmpA, NULL, 0, c->tmpA,
-                     c->p->prm.correction_scale, 1);
+        rc = ufoir__fp_full(c->p, &c->fs, in, c->tmpA, NULL, 0, c->tmpA, c->p->prm.correction_scale, 1);
     if (!rc)
         rc = udev_bp(d, &c->g, c->p->subsets, (int) c->p->n_subsets, c->tmpA, NULL, NULL, 0, NULL, c->tmpAt,
                      c->p->prm.relaxation, 1);
@@ -863,7 +859,7 @@ int ufoir_sbtv_process(ufoir_projector *proj, const ufoir_sbtv_params *prm, cons
     c.tmpAt = buf[12];
     c.tmpD = buf[13];
     c.tmpDxt = buf[14];
-    c.inT = buf[15];
+    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &c.fs, 1));
     float *fbp = buf[16], *up = buf[17], *bvec = buf[18], *bx = buf[19], *by = buf[20], *dx = buf[21];
     float *dy = buf[22], *tmpx = buf[23], *tmpy = buf[24], *tmp = buf[25];
 
@@ -924,6 +920,7 @@ done:
         ufoir__free(ctx, buf[i]);
     ufoir__free(ctx, f);
     ufoir__free(ctx, c.tmpA);
+    ufoir__fp_scratch_free(proj, &c.fs);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bo);
     udev_sync(d);

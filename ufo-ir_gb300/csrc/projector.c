@@ -86,8 +86,12 @@ static void free_geometry(ufoir_projector *p)
         udev_free(p->ctx->dev, p->d_cos);
     if (p->d_dir)
         udev_free(p->ctx->dev, p->d_dir);
+    if (p->d_tiles)
+        udev_free(p->ctx->dev, p->d_tiles);
     p->d_sin = p->d_cos = NULL;
     p->d_dir = NULL;
+    p->d_tiles = NULL;
+    p->tiles_valid = 0;
     p->lut_cap = 0;
     p->have_geometry = 0;
 }
@@ -196,6 +200,7 @@ static int build_geometry(ufoir_projector *p, unsigned int n_angles)
     p->n_angles = n_angles;
     p->lut_step = step;
     p->have_geometry = 1;
+    p->tiles_valid = 0;
     return UFOIR_OK;
 }
 
@@ -273,23 +278,113 @@ int ufoir_projector_get_subsets(const ufoir_projector *proj, const ufoir_subset 
     return UFOIR_OK;
 }
 
-/* Forward projection of all angles of n_slices volumes (accumulating):
- * sino = sino + scale * A vol. Needs a transposed copy for horizontal rays. */
-static int fp_all(ufoir_projector *p, const float *dvol, float *dsino, size_t n_slices)
+/* Angle tiles of the tiled forward projector: runs of at most A angles that
+ * never cross a direction boundary (the full subsets, cut into pieces). */
+static int ensure_tiles(ufoir_projector *p)
 {
     ufoir_ctx *ctx = p->ctx;
-    udev_geom g;
-    ufoir__projector_geom(p, &g);
-    const size_t nv = (size_t) p->n_dets * p->n_dets;
-    float *volT = NULL;
-    int rc = ufoir__alloc(ctx, &volT, nv * n_slices);
+    const int A = udev_fp_tile_angles(ctx->dev, (int) p->n_dets);
+    if (A <= 0)
+        return UFOIR_ERR_UNSUPPORTED;
+    if (p->tiles_valid && p->tiles_A == A)
+        return UFOIR_OK;
+    int count = 0;
+    for (unsigned int i = 0; i < p->n_subsets; i++)
+        count += (int) ((p->subsets[i].n + (unsigned int) A - 1) / (unsigned int) A);
+    int *h = (int *) malloc(sizeof(int) * 4 * (size_t) (count ? count : 1));
+    if (!h)
+        return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+    int t = 0;
+    for (unsigned int i = 0; i < p->n_subsets; i++)
+        for (unsigned int a = 0; a < p->subsets[i].n; a += (unsigned int) A, t++) {
+            const unsigned int left = p->subsets[i].n - a;
+            h[4 * t + 0] = (int) (p->subsets[i].offset + a);
+            h[4 * t + 1] = (int) (left < (unsigned int) A ? left : (unsigned int) A);
+            h[4 * t + 2] = p->subsets[i].direction;
+            h[4 * t + 3] = 0;
+        }
+    if (p->d_tiles)
+        udev_free(ctx->dev, p->d_tiles);
+    p->d_tiles = NULL;
+    p->tiles_valid = 0;
+    int rc = udev_malloc(ctx->dev, &p->d_tiles, sizeof(int) * 4 * (size_t) (count ? count : 1));
+    if (!rc)
+        rc = udev_memcpy(ctx->dev, p->d_tiles, h, sizeof(int) * 4 * (size_t) count);
+    free(h);
     if (rc)
         return rc;
-    rc = udev_transpose(ctx->dev, dvol, volT, (int) p->n_dets, (int) n_slices);
+    p->n_tiles = count;
+    p->tiles_A = A;
+    p->tiles_valid = 1;
+    return UFOIR_OK;
+}
+
+int ufoir__fp_scratch_alloc(ufoir_projector *p, ufoir_fp_scratch *s, size_t slices)
+{
+    const size_t n = p->n_dets, pitch = (size_t) udev_fp_pitch((int) n);
+    s->P = s->TP = NULL;
+    s->slices = slices;
+    const size_t count = n * pitch * slices;
+    int rc = ufoir__alloc(p->ctx, &s->P, count);
     if (!rc)
-        rc = udev_fp(ctx->dev, &g, 0, (int) p->n_angles, -1, dvol, volT, dsino, NULL, 0, dsino,
-                     p->prm.correction_scale, (int) n_slices);
-    ufoir__free(ctx, volT);
+        rc = ufoir__alloc(p->ctx, &s->TP, count);
+    if (!rc)
+        rc = udev_memset(p->ctx->dev, s->P, 0, count * sizeof(float));
+    if (!rc)
+        rc = udev_memset(p->ctx->dev, s->TP, 0, count * sizeof(float));
+    if (rc)
+        ufoir__fp_scratch_free(p, s);
+    return rc;
+}
+
+void ufoir__fp_scratch_free(ufoir_projector *p, ufoir_fp_scratch *s)
+{
+    ufoir__free(p->ctx, s->P);
+    ufoir__free(p->ctx, s->TP);
+    s->P = s->TP = NULL;
+}
+
+int ufoir__fp_prepare(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, int n_slices)
+{
+    if (udev_fp_tile_angles(p->ctx->dev, (int) p->n_dets) > 0)
+        return udev_pad_transpose(p->ctx->dev, vol, s->P, s->TP, (int) p->n_dets, n_slices);
+    /* the tiled kernel cannot serve this size: plain transpose for the row kernel */
+    return udev_transpose(p->ctx->dev, vol, s->TP, (int) p->n_dets, n_slices);
+}
+
+int ufoir__fp_project(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, const float *src, const float *w,
+                      int w_shared, float *out, float scale, int n_slices)
+{
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    const int rc = ensure_tiles(p);
+    if (rc == UFOIR_OK)
+        return udev_fp_tiles(p->ctx->dev, &g, p->d_tiles, p->n_tiles, s->P, s->TP, src, w, w_shared, out, scale,
+                             n_slices);
+    if (rc != UFOIR_ERR_UNSUPPORTED)
+        return rc;
+    return udev_fp(p->ctx->dev, &g, 0, (int) p->n_angles, -1, vol, s->TP, src, w, w_shared, out, scale, n_slices);
+}
+
+int ufoir__fp_full(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, const float *src, const float *w,
+                   int w_shared, float *out, float scale, int n_slices)
+{
+    int rc = ufoir__fp_prepare(p, s, vol, n_slices);
+    if (!rc)
+        rc = ufoir__fp_project(p, s, vol, src, w, w_shared, out, scale, n_slices);
+    return rc;
+}
+
+/* Forward projection of all angles of n_slices volumes (accumulating):
+ * sino = sino + scale * A vol. */
+static int fp_all(ufoir_projector *p, const float *dvol, float *dsino, size_t n_slices)
+{
+    ufoir_fp_scratch s;
+    int rc = ufoir__fp_scratch_alloc(p, &s, n_slices);
+    if (rc)
+        return rc;
+    rc = ufoir__fp_full(p, &s, dvol, dsino, NULL, 0, dsino, p->prm.correction_scale, (int) n_slices);
+    ufoir__fp_scratch_free(p, &s);
     return rc;
 }
 

@@ -66,6 +66,25 @@ int udev_fp(udev *d, const udev_geom *g, int a0, int na, int dir_override,
 /* Transpose n x n slices. */
 int udev_transpose(udev *d, const float *in, float *out, int n, int n_slices);
 
+/* ---- Tiled forward projector (all angles, shared-memory row streaming) ---- */
+/* Row pitch (floats, multiple of 4) of the padded images: 2 zero columns,
+ * n values, at least 2 zero columns. */
+int udev_fp_pitch(int n);
+/* Angles per CTA tile for n detectors; 0 if the tiled kernel cannot serve n. */
+int udev_fp_tile_angles(udev *d, int n);
+/* Writes the padded copy and the padded transpose of n_slices n x n images
+ * into buffers of n * pitch floats per slice whose pad columns are zero. */
+int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int n, int n_slices);
+/* Same contract as udev_fp over all angles, reading the padded images.
+ * d_tiles: device array of int4 {first angle, count, direction, 0}. */
+int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, const float *volP,
+                  const float *volTP, const float *src, const float *w, int w_shared, float *out,
+                  float scale, int n_slices);
+int udev_memset(udev *d, void *p, int value, size_t bytes);
+/* Returns UFOIR_ERR_TIMEOUT (and clears the word) if a kernel recorded a
+ * bounded-wait timeout since the last check; waits for the stream. */
+int udev_take_kernel_error(udev *d);
+
 /* Pixel-driven backprojection over a list of subsets:
  *   v = base ? base : 0;  for each subset: v = v + relax * sum_{angles} lerp(sino)
  *   if cw: v = v * cw;  if add: v = v + add;  dst = v

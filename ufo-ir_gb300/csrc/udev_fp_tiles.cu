@@ -1,0 +1,359 @@
+/*
+ * udev_fp_tiles.cu - the forward projector for whole angle sets (every
+ * method's A x), streaming image rows through shared memory.
+ *
+ * Layout: the volume (for vertical rays) and its transpose (for horizontal
+ * rays) are first written as padded copies, each row [2 zeros | n values |
+ * zeros] of `pitch` floats (pitch % 4 == 0), so that every ray of either
+ * direction walks the rows of a row-major image and a zero border needs no
+ * bounds checks. One CTA owns a tile of up to A consecutive angles of one
+ * direction and all n detectors (J per thread, lanes on adjacent
+ * detectors). All of its A*n rays advance row by row in lockstep; chunks of
+ * K rows (K | 64) are brought into shared memory by a single 1-D TMA bulk
+ * copy each (cp.async.bulk + mbarrier, double buffered), and every row in
+ * shared memory is sampled by all A*n rays, so the image is read from L2
+ * once per tile instead of once per ray.
+ *
+ * Arithmetic is the reference's: per ray, the float coordinate recurrence,
+ * one linear-filter sample per row with (1 - t) * T0 + t * T1, samples
+ * summed in blocks of 64, then sino = src + scale * sum
+ * (projector-parallel-joseph.cl:36-156). floor() is taken with a
+ * round-toward-minus-infinity add of 1.5 * 2^23 instead of conversion
+ * instructions; for |x| < 2^22 it is exact.
+ */
+#include <cuda_runtime.h>
+
+#include "joseph.cuh"
+#include "tma.cuh"
+#include "udev_internal.cuh"
+
+namespace {
+
+constexpr int kPadL = 2;
+constexpr float kFloorMagic = 12582912.0f;      /* 1.5 * 2^23 */
+constexpr int kFloorMagicBits = 0x4B400000;
+
+struct FpTileArgs {
+    const float *volP;
+    const float *volTP;
+    const float *src;
+    const float *w;
+    float *out;
+    const float *sinv;
+    const float *cosv;
+    const int4 *tiles;     /* {first angle, angle count, direction, 0} */
+    int n;
+    int pitch;
+    int rows_per_chunk;
+    float axis;
+    float scale;
+    long long volp_stride;
+    long long sino_stride;
+    long long w_stride;
+    int *err;
+};
+
+template <int J, int A>
+__global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
+    float *stage0 = reinterpret_cast<float *>(smem_raw + 128);
+    const int K = P.rows_per_chunk;
+    const int pitch = P.pitch;
+    const size_t stage_floats = (size_t) K * pitch;
+
+    const int4 tile = P.tiles[blockIdx.x];
+    const int slice = (int) blockIdx.y;
+    const int n = P.n;
+    const int dir = tile.z;
+    const float *img = (dir == 0 ? P.volTP : P.volP) + (size_t) slice * P.volp_stride;
+
+    const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
+    float c[A][J], inner[A][J], sum[A][J], stp[A];
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+        stp[a] = 0.0f;
+        float det_step = 0.0f;
+        if (a < tile.y) {
+            const int angle = tile.x + a;
+            joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, stp[a]);
+        }
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const int s = (int) threadIdx.x + j * (int) blockDim.x;
+            c[a][j] = (a < tile.y && s < n) ? joseph::ray_start(kc, s, n, det_step, stp[a]) : 0.0f;
+            inner[a][j] = 0.0f;
+            sum[a][j] = 0.0f;
+        }
+    }
+
+    const int nchunks = (n + K - 1) / K;
+    if (threadIdx.x == 0) {
+        tma::mbar_init(&bars[0], 1);
+        tma::mbar_init(&bars[1], 1);
+        tma::fence_mbar_init();
+    }
+    __syncthreads();
+
+    int issued = 0;
+    if (threadIdx.x == 0) {
+        for (; issued < 2 && issued < nchunks; ++issued) {
+            const int r0 = issued * K;
+            const uint32_t bytes = (uint32_t) (min(K, n - r0) * pitch) * 4u;
+            tma::mbar_arrive_expect_tx(&bars[issued & 1], bytes);
+            tma::bulk_g2s(stage0 + (issued & 1) * stage_floats, img + (size_t) r0 * pitch, bytes,
+                          &bars[issued & 1]);
+        }
+    }
+
+    const float hi = (float) n + 0.5f;
+    bool ok = true;
+    int waited = 0;
+    for (int ch = 0; ch < nchunks; ++ch) {
+        const int st = ch & 1;
+        if (ok) {
+            ok = tma::mbar_wait(&bars[st], (uint32_t) ((ch >> 1) & 1), P.err, tma::kErrWaitTimeout);
+            waited = ch + 1;
+        }
+        const int r0 = ch * K;
+        const int rows = min(K, n - r0);
+        if (ok) {
+            const float *sbuf = stage0 + st * stage_floats + kPadL;
+            for (int r = 0; r < rows; ++r) {
+                const float *row = sbuf + (size_t) r * pitch;
+#pragma unroll
+                for (int a = 0; a < A; ++a) {
+#pragma unroll
+                    for (int j = 0; j < J; ++j) {
+                        float cm = __fsub_rn(c[a][j], 0.5f);
+                        cm = fminf(fmaxf(cm, -1.5f), hi);
+                        const float y = __fadd_rd(cm, kFloorMagic);
+                        const float fi = __fsub_rn(y, kFloorMagic);
+                        const int i0 = __float_as_int(y) - kFloorMagicBits;
+                        const float t = __fsub_rn(cm, fi);
+                        inner[a][j] = __fadd_rn(inner[a][j], joseph::lerp(t, row[i0], row[i0 + 1]));
+                        c[a][j] = __fadd_rn(c[a][j], stp[a]);
+                    }
+                }
+                if (((r0 + r + 1) & 63) == 0) {
+#pragma unroll
+                    for (int a = 0; a < A; ++a)
+#pragma unroll
+                        for (int j = 0; j < J; ++j) {
+                            sum[a][j] = __fadd_rn(sum[a][j], inner[a][j]);
+                            inner[a][j] = 0.0f;
+                        }
+                }
+            }
+        }
+        ok = __syncthreads_and(ok) != 0;
+        if (threadIdx.x == 0 && ok && issued < nchunks) {
+            /* every thread is done with this stage: refill it */
+            tma::fence_proxy_async_smem();
+            const int r0n = issued * K;
+            const uint32_t bytes = (uint32_t) (min(K, n - r0n) * pitch) * 4u;
+            tma::mbar_arrive_expect_tx(&bars[issued & 1], bytes);
+            tma::bulk_g2s(stage0 + (issued & 1) * stage_floats, img + (size_t) r0n * pitch, bytes,
+                          &bars[issued & 1]);
+            ++issued;
+        }
+    }
+    if (!ok) {
+        /* a copy did not arrive in time: drain what was issued, write nothing */
+        if (threadIdx.x == 0)
+            for (int ch = waited; ch < issued; ++ch)
+                tma::mbar_wait(&bars[ch & 1], (uint32_t) ((ch >> 1) & 1), P.err, tma::kErrDrainTimeout);
+        return;
+    }
+
+    if ((n & 63) != 0) {
+#pragma unroll
+        for (int a = 0; a < A; ++a)
+#pragma unroll
+            for (int j = 0; j < J; ++j)
+                sum[a][j] = __fadd_rn(sum[a][j], inner[a][j]);
+    }
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+        if (a >= tile.y)
+            continue;
+        const int angle = tile.x + a;
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const int s = (int) threadIdx.x + j * (int) blockDim.x;
+            if (s >= n)
+                continue;
+            const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + s;
+            float result = P.src[oidx];
+            if (!joseph::detector_inactive(kc, s))
+                result = __fadd_rn(result, __fmul_rn(sum[a][j], P.scale));
+            if (P.w)
+                result = __fmul_rn(result, P.w[(size_t) slice * P.w_stride + (size_t) angle * n + s]);
+            P.out[oidx] = result;
+        }
+    }
+}
+
+/* Writes the padded copy and the padded transpose of n x n slices; the pad
+ * columns are left as they are (zeroed once when the buffers are made). */
+__global__ void __launch_bounds__(256) pad_transpose_kernel(const float *__restrict__ in, float *__restrict__ outP,
+                                                            float *__restrict__ outTP, int n, int pitch,
+                                                            long long in_stride, long long out_stride)
+{
+    __shared__ float tile[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    const float *src = in + (size_t) blockIdx.z * in_stride;
+    float *dp = outP + (size_t) blockIdx.z * out_stride;
+    float *dt = outTP + (size_t) blockIdx.z * out_stride;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = bx + threadIdx.x, y = by + j;
+        if (x < n && y < n) {
+            const float v = src[(size_t) y * n + x];
+            tile[j][threadIdx.x] = v;
+            dp[(size_t) y * pitch + kPadL + x] = v;
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = by + threadIdx.x, y = bx + j;
+        if (x < n && y < n)
+            dt[(size_t) y * pitch + kPadL + x] = tile[threadIdx.x][j];
+    }
+}
+
+struct TileCfg {
+    int J, A, threads, K;
+    size_t smem;
+};
+
+constexpr int kMaxTileThreads = 768;
+
+TileCfg tile_cfg(int n, int smem_optin)
+{
+    TileCfg c;
+    c.J = n <= 768 ? 1 : (n <= 1536 ? 2 : (n <= 3072 ? 4 : 8));
+    c.A = c.J <= 2 ? 8 : (c.J == 4 ? 4 : 2);
+    c.threads = (int) (((n + c.J - 1) / c.J + 31) / 32 * 32);
+    const int pitch = udev_fp_pitch(n);
+    c.K = 32;
+    while (c.K > 4 && 128 + 2 * (size_t) c.K * pitch * 4 > (size_t) smem_optin)
+        c.K /= 2;
+    c.smem = 128 + 2 * (size_t) c.K * pitch * 4;
+    return c;
+}
+
+template <int J, int A>
+int launch_tiles(udev *d, const FpTileArgs &args, int n_tiles, int n_slices, const TileCfg &cfg)
+{
+    for (int done = 0; done < n_slices;) {
+        const int chunk = n_slices - done > 65535 ? 65535 : n_slices - done;
+        FpTileArgs B = args;
+        B.volP += (size_t) done * args.volp_stride;
+        B.volTP += (size_t) done * args.volp_stride;
+        B.src += (size_t) done * args.sino_stride;
+        B.out += (size_t) done * args.sino_stride;
+        if (B.w)
+            B.w += (size_t) done * args.w_stride;
+        fp_tiles_kernel<J, A><<<dim3((unsigned int) n_tiles, (unsigned int) chunk), cfg.threads, cfg.smem,
+                                d->stream>>>(B);
+        int rc = udev_after_launch(d, "fp_tiles_kernel");
+        if (rc)
+            return rc;
+        done += chunk;
+    }
+    return UFOIR_OK;
+}
+
+}  // namespace
+
+extern "C" int udev_fp_pitch(int n)
+{
+    return (n + kPadL + 2 + 3) / 4 * 4;
+}
+
+static bool tiles_supported(const TileCfg &cfg, int smem_optin)
+{
+    return cfg.threads <= kMaxTileThreads && cfg.smem <= (size_t) smem_optin && cfg.K >= 8;
+}
+
+extern "C" int udev_fp_tile_angles(udev *d, int n)
+{
+    const TileCfg cfg = tile_cfg(n, d->smem_optin);
+    return tiles_supported(cfg, d->smem_optin) ? cfg.A : 0;
+}
+
+int udev_kernels_init(udev *d)
+{
+    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       d->smem_optin));
+    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       d->smem_optin));
+    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       d->smem_optin));
+    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       d->smem_optin));
+    return UFOIR_OK;
+}
+
+extern "C" int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int n, int n_slices)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    const int pitch = udev_fp_pitch(n);
+    for (int done = 0; done < n_slices;) {
+        const int chunk = n_slices - done > 65535 ? 65535 : n_slices - done;
+        dim3 grid(udev_div_up(n, 32), udev_div_up(n, 32), (unsigned int) chunk);
+        pad_transpose_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(
+            vol + (size_t) done * n * n, volP + (size_t) done * n * pitch, volTP + (size_t) done * n * pitch, n, pitch,
+            (long long) n * n, (long long) n * pitch);
+        int rc = udev_after_launch(d, "pad_transpose_kernel");
+        if (rc)
+            return rc;
+        done += chunk;
+    }
+    return UFOIR_OK;
+}
+
+extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, const float *volP,
+                             const float *volTP, const float *src, const float *w, int w_shared, float *out,
+                             float scale, int n_slices)
+{
+    if (n_slices <= 0 || n_tiles <= 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    const int n = g->n_dets;
+    const TileCfg cfg = tile_cfg(n, d->smem_optin);
+    if (!tiles_supported(cfg, d->smem_optin)) {
+        udev_set_error(d, "fp_tiles: n_dets %d needs %d threads / %zu B shared memory", n, cfg.threads, cfg.smem);
+        return UFOIR_ERR_UNSUPPORTED;
+    }
+    FpTileArgs A;
+    A.volP = volP;
+    A.volTP = volTP;
+    A.src = src;
+    A.w = w;
+    A.out = out;
+    A.sinv = g->d_sin;
+    A.cosv = g->d_cos;
+    A.tiles = static_cast<const int4 *>(d_tiles);
+    A.n = n;
+    A.pitch = udev_fp_pitch(n);
+    A.rows_per_chunk = cfg.K;
+    A.axis = g->axis;
+    A.scale = scale;
+    A.volp_stride = (long long) n * A.pitch;
+    A.sino_stride = (long long) g->n_angles * n;
+    A.w_stride = w_shared ? 0 : A.sino_stride;
+    A.err = d->d_err;
+    switch (cfg.J * 16 + cfg.A) {
+    case 1 * 16 + 8: return launch_tiles<1, 8>(d, A, n_tiles, n_slices, cfg);
+    case 2 * 16 + 8: return launch_tiles<2, 8>(d, A, n_tiles, n_slices, cfg);
+    case 4 * 16 + 4: return launch_tiles<4, 4>(d, A, n_tiles, n_slices, cfg);
+    case 8 * 16 + 2: return launch_tiles<8, 2>(d, A, n_tiles, n_slices, cfg);
+    default:
+        udev_set_error(d, "fp_tiles: no kernel for J=%d A=%d", cfg.J, cfg.A);
+        return UFOIR_ERR_UNSUPPORTED;
+    }
+}

@@ -25,7 +25,12 @@ struct udev {
     size_t red_out_cap = 0;
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_stop = nullptr;
+    int *d_err = nullptr;           /* kernel error word (bounded-wait timeouts) */
+    int *h_err = nullptr;
 };
+
+/* One-time kernel attribute setup (dynamic shared memory opt-in). */
+int udev_kernels_init(udev *d);
 
 #define UDEV_BIND(d)                                                                   \
     do {                                                                               \

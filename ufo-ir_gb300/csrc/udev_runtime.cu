@@ -81,6 +81,12 @@ int udev_create(int device, udev **out, char *err, size_t errlen)
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
     }
     cudaGetLastError();
+    if (cudaMalloc(&d->d_err, sizeof(int)) != cudaSuccess || cudaMemset(d->d_err, 0, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&d->h_err, sizeof(int)) != cudaSuccess || udev_kernels_init(d) != UFOIR_OK) {
+        snprintf(err, errlen, "context setup failed: %s", d->err[0] ? d->err : cudaGetErrorString(cudaGetLastError()));
+        udev_destroy(d);
+        return UFOIR_ERR_CUDA;
+    }
     *out = d;
     return UFOIR_OK;
 }
@@ -101,7 +107,12 @@ void udev_destroy(udev *d)
         cudaEventDestroy(d->ev_start);
     if (d->ev_stop)
         cudaEventDestroy(d->ev_stop);
-    cudaStreamDestroy(d->stream);
+    if (d->d_err)
+        cudaFree(d->d_err);
+    if (d->h_err)
+        cudaFreeHost(d->h_err);
+    if (d->stream)
+        cudaStreamDestroy(d->stream);
     delete d;
 }
 
@@ -215,6 +226,30 @@ int udev_memcpy(udev *d, void *dst, const void *src, size_t bytes)
     if (rc)
         return rc;
     return udev_sync(d);
+}
+
+int udev_memset(udev *d, void *p, int value, size_t bytes)
+{
+    if (bytes == 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaMemsetAsync(p, value, bytes, d->stream));
+    return UFOIR_OK;
+}
+
+int udev_take_kernel_error(udev *d)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaMemcpyAsync(d->h_err, d->d_err, sizeof(int), cudaMemcpyDeviceToHost, d->stream));
+    UDEV_CHECK(d, cudaStreamSynchronize(d->stream));
+    const int code = *d->h_err;
+    if (code == 0)
+        return UFOIR_OK;
+    UDEV_CHECK(d, cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream));
+    UDEV_CHECK(d, cudaStreamSynchronize(d->stream));
+    udev_set_error(d, "a kernel gave up waiting for a shared-memory copy (code %d); results of that call are invalid",
+                   code);
+    return UFOIR_ERR_TIMEOUT;
 }
 
 int udev_timer_begin(udev *d)

@@ -451,7 +451,7 @@ class SirtBatch:
     def profile(self):
         ms = (C.c_float * 3)()
         self.proj.ctx._check(lib().ufoir_sirt_batch_profile(self.handle, ms))
-        return {"transpose": ms[0], "fp": ms[1], "bp": ms[2]}
+        return {"prepare": ms[0], "fp": ms[1], "bp": ms[2]}
 
     def close(self):
         if self.handle:
