@@ -300,8 +300,8 @@ def run_ufoir(args, dist):
     dom = "fp" if kernel_ms["fp"] >= kernel_ms["bp"] else "bp"
     dom_bytes = fp_bytes if dom == "fp" else bp_bytes
     achieved = dom_bytes / (kernel_ms[dom] / 1e3) / 1e9
-    traffic = ncu_traffic().get({"fp": "fp_rows_kernel", "bp": "bp_gather_kernel"}[dom])
-    roofline = {"bound": "hbm", "kernel": {"fp": "fp_rows_kernel", "bp": "bp_gather_kernel"}[dom],
+    traffic = ncu_traffic().get({"fp": "fp_tiles_kernel", "bp": "bp_tiles_kernel"}[dom])
+    roofline = {"bound": "hbm", "kernel": {"fp": "fp_tiles_kernel", "bp": "bp_tiles_kernel"}[dom],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "traffic": traffic * S if traffic else None,
@@ -319,7 +319,7 @@ def run_ufoir(args, dist):
                    "Poisson noise I0=1e5, log",
            "config": {"workload": "batched SIRT, 64 slices x 1448^2 grid (1024^2 phantoms), 1200 angles, 1448 bins",
                       "slices_per_gpu": S, "n_dets": n, "n_angles": na, "relaxation_factor": RELAX,
-                      "step": "one SIRT iteration over all slices, one CUDA graph (transpose+FP+BP)",
+                      "step": "one SIRT iteration over all slices, one CUDA graph (pad+transpose, FP, BP)",
                       "l2": "inputs larger than L2 (about 3 GB resident working set per GPU)",
                       "parallelism": "replicas: slices sharded across ranks, no collective"},
            "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "roofline": roofline,

@@ -80,6 +80,11 @@ int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int
 int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, const float *volP,
                   const float *volTP, const float *src, const float *w, int w_shared, float *out,
                   float scale, int n_slices);
+/* Backprojection with shared-memory sinogram windows (udev_bp uses it for
+ * 16 or more angles); same contract as udev_bp, at most 16 subsets. */
+int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
+                  const float *sino, const float *base, const float *cw, int cw_shared,
+                  const float *add, float *dst, float relax, int n_slices);
 int udev_memset(udev *d, void *p, int value, size_t bytes);
 /* Returns UFOIR_ERR_TIMEOUT (and clears the word) if a kernel recorded a
  * bounded-wait timeout since the last check; waits for the stream. */

@@ -263,13 +263,18 @@ extern "C" int udev_bp(udev *d, const udev_geom *g, const ufoir_subset *subsets,
 {
     if (n_slices <= 0)
         return UFOIR_OK;
+    size_t total = 0;
     for (int i = 0; i < n_subsets; i++) {
         if (subsets[i].offset + (size_t) subsets[i].n > (size_t) g->n_angles) {
             udev_set_error(d, "bp: subset [%u, %u) outside [0, %d)", subsets[i].offset,
                            subsets[i].offset + subsets[i].n, g->n_angles);
             return UFOIR_ERR_INVALID;
         }
+        total += subsets[i].n;
     }
+    /* many angles: the tiled kernel (shared-memory sinogram windows) */
+    if (total >= 16 && n_subsets <= 16)
+        return udev_bp_tiles(d, g, subsets, n_subsets, sino, base, cw, cw_shared, add, dst, relax, n_slices);
     UDEV_BIND(d);
     BpArgs A;
     A.sino = sino;
