@@ -286,6 +286,37 @@ UFOIR_API int ufoir_l1_norm(ufoir_ctx *ctx, const float *v, size_t w, size_t h, 
 UFOIR_API int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, size_t w,
                                 size_t h, int norm_mode, float *out);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free L1 norm. No counterpart in the reference.                */
+/*                                                                          */
+/* For callers that cannot allocate device memory at the point where they  */
+/* need the norm: code running while its own stream is captured into a CUDA */
+/* graph (allocation is not capturable), code whose GPU memory belongs to   */
+/* another allocator or sits under a hard per-process limit, and loops that */
+/* must not take the allocator's locks. It computes what ufoir_l1_norm      */
+/* computes with UFOIR_NORM_FP64 (same result bit for bit), for n_slices     */
+/* slices of `count` floats stored back to back, but keeps its partial sums */
+/* in a fixed device array inside the library instead of allocating:       */
+/*   - the array holds UFOIR_NOALLOC_MAX_SLICES x 512 doubles (256 KiB) and  */
+/*     every GPU that loads the library keeps it until the process exits;   */
+/*   - n_slices > UFOIR_NOALLOC_MAX_SLICES is rejected with                 */
+/*     UFOIR_ERR_INVALID and nothing is launched;                           */
+/*   - the first call on a device looks up that array's device address      */
+/*     (cudaGetSymbolAddress, once per device, with the caller's current    */
+/*     device); make that first call before any stream capture;             */
+/*   - all calls share the array, so calls whose work overlaps on the GPU   */
+/*     (different streams without ordering between them) race and give      */
+/*     wrong results; each call overwrites every partial it reads, so       */
+/*     nothing needs clearing between calls.                                */
+/* d_v (input) and d_out (n_slices floats, output) are device memory of the */
+/* current device; the work is queued on `stream` (a cudaStream_t, NULL =   */
+/* the default stream) and d_out is valid once the stream reaches it. No   */
+/* cudaMalloc, cudaFree or allocating library call is made.                 */
+/* ------------------------------------------------------------------------ */
+#define UFOIR_NOALLOC_MAX_SLICES 64
+UFOIR_API int ufoir_l1_norm_fp64_noalloc(const float *d_v, size_t count, unsigned int n_slices,
+                                         float *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
