@@ -152,10 +152,10 @@ def ncu_traffic():
     return {}
 
 
-def make_inputs(ufoir, ctx, proj, rank):
+def make_inputs(ufoir, ctx, proj, rank, S):
     """Phantoms -> Joseph FP on the GPU -> Poisson noise -> device sinograms."""
     from ufoir import synth
-    n, na, S = N_DETS, N_ANGLES, SLICES
+    n, na = N_DETS, N_ANGLES
     vols = np.empty((S, n, n), np.float32)
     for i in range(S):
         vols[i] = synth.ellipse_phantom(n, PHANTOM, 10, seed=2000 + rank * S + i)
@@ -236,11 +236,11 @@ def run_reference(args, dist):
 
 def run_ufoir(args, dist):
     import ufoir
-    n, na, S = N_DETS, N_ANGLES, SLICES
+    n, na, S = N_DETS, N_ANGLES, args.slices
     ctx = ufoir.Context(dist.local)
     step = float(np.float32(np.pi / na))
     proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=0)
-    d_sino, d_vol, noisy = make_inputs(ufoir, ctx, proj, dist.rank)
+    d_sino, d_vol, noisy = make_inputs(ufoir, ctx, proj, dist.rank, S)
 
     batch = ufoir.SirtBatch(proj, d_sino, d_vol, relaxation_factor=RELAX)
     for _ in range(max(args.warmup, 0)):
@@ -263,33 +263,9 @@ def run_ufoir(args, dist):
     value = S * args.steps * dist.world / (ms_max / 1e3)
     batch.close()
 
-    # e2e through the public API with host (pinned) buffers
-    h_sino = ctx.pinned_empty((S, na, n))
-    h_sino[...] = noisy
-    h_vol = ctx.pinned_empty((S, n, n))
-    ufoir.sirt(proj, h_sino, h_vol, num_iterations=1, relaxation_factor=RELAX)   # warm
-    dist.barrier()
-    t0 = time.perf_counter()
-    ufoir.sirt(proj, h_sino, h_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
-    e2e_s = dist.max(time.perf_counter() - t0)
-    e2e = {"value": S * E2E_ITERS * dist.world / e2e_s, "unit": "slice-iters/s",
-           "h2d_bytes_per_step": int(h_sino.nbytes), "d2h_bytes_per_step": int(h_vol.nbytes),
-           "call": f"ufoir_sirt_process(host buffers, {S} slices, num-iterations {E2E_ITERS})",
-           "seconds": e2e_s}
-
-    # one job per launch sequence (plain per-job path) vs the batched call, same API, device data
-    jobs = 8
-    t0 = time.perf_counter()
-    for i in range(jobs):
-        ufoir.sirt(proj, d_sino.slice(i), d_vol.slice(i), num_iterations=E2E_ITERS, relaxation_factor=RELAX)
-    plain_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    ufoir.sirt(proj, d_sino, d_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
-    batched_s = time.perf_counter() - t0
-    per_job = {"plain_per_job": {"value": jobs * E2E_ITERS / plain_s, "unit": "slice-iters/s",
-                                 "how": f"{jobs} single-slice ufoir_sirt_process calls, {E2E_ITERS} iterations each"},
-               "batched_call": {"value": S * E2E_ITERS / batched_s, "unit": "slice-iters/s",
-                                "how": f"one ufoir_sirt_process call on {S} slices, {E2E_ITERS} iterations"}}
+    e2e, per_job = None, {}
+    if not args.quick:
+        e2e, per_job = end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S)
 
     # roofline of the dominant kernel (live CUDA-event durations above)
     peak, peak_kind = measured_peaks()
@@ -317,20 +293,54 @@ def run_ufoir(args, dist):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic: seeded random-ellipse 1024^2 phantoms in a 1448^2 grid, Joseph FP, "
                    "Poisson noise I0=1e5, log",
-           "config": {"workload": "batched SIRT, 64 slices x 1448^2 grid (1024^2 phantoms), 1200 angles, 1448 bins",
+           "config": {"workload": f"batched SIRT, {S} slices x 1448^2 grid (1024^2 phantoms), 1200 angles, "
+                                  "1448 bins",
                       "slices_per_gpu": S, "n_dets": n, "n_angles": na, "relaxation_factor": RELAX,
                       "step": "one SIRT iteration over all slices, one CUDA graph (pad+transpose, FP, BP)",
                       "l2": "inputs larger than L2 (about 3 GB resident working set per GPU)",
                       "parallelism": "replicas: slices sharded across ranks, no collective"},
            "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "roofline": roofline,
            "kernel_ms": kernel_ms, "sample_rate": sample_rate, **per_job}
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and not args.quick:
         out["cpu_baseline"] = cpu_baseline(noisy[0])
     d_sino.close()
     d_vol.close()
     proj.close()
     ctx.close()
     return out if dist.rank == 0 else None
+
+
+def end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S):
+    """e2e through the public API with host buffers, and one job per launch vs one batched call."""
+    n, na = N_DETS, N_ANGLES
+    # e2e through the public API with host (pinned) buffers
+    h_sino = ctx.pinned_empty((S, na, n))
+    h_sino[...] = noisy
+    h_vol = ctx.pinned_empty((S, n, n))
+    ufoir.sirt(proj, h_sino, h_vol, num_iterations=1, relaxation_factor=RELAX)   # warm
+    dist.barrier()
+    t0 = time.perf_counter()
+    ufoir.sirt(proj, h_sino, h_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = {"value": S * E2E_ITERS * dist.world / e2e_s, "unit": "slice-iters/s",
+           "h2d_bytes_per_step": int(h_sino.nbytes), "d2h_bytes_per_step": int(h_vol.nbytes),
+           "call": f"ufoir_sirt_process(host buffers, {S} slices, num-iterations {E2E_ITERS})",
+           "seconds": e2e_s}
+
+    # one job per launch sequence (plain per-job path) vs the batched call, same API, device data
+    jobs = 8
+    t0 = time.perf_counter()
+    for i in range(jobs):
+        ufoir.sirt(proj, d_sino.slice(i), d_vol.slice(i), num_iterations=E2E_ITERS, relaxation_factor=RELAX)
+    plain_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ufoir.sirt(proj, d_sino, d_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
+    batched_s = time.perf_counter() - t0
+    per_job = {"plain_per_job": {"value": jobs * E2E_ITERS / plain_s, "unit": "slice-iters/s",
+                                 "how": f"{jobs} single-slice ufoir_sirt_process calls, {E2E_ITERS} iterations each"},
+               "batched_call": {"value": S * E2E_ITERS / batched_s, "unit": "slice-iters/s",
+                                "how": f"one ufoir_sirt_process call on {S} slices, {E2E_ITERS} iterations"}}
+    return e2e, per_job
 
 
 def main():
@@ -340,6 +350,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ufoir", choices=["ufoir", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slices", type=int, default=SLICES, help="slices per GPU (64 = the headline workload)")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the resident timed steps (skip e2e, per-job comparison, CPU baseline)")
     args = ap.parse_args()
     dist = Dist()
     try:

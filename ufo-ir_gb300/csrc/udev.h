@@ -137,6 +137,17 @@ int udev_dot(udev *d, const float *a, const float *b, size_t w, size_t h, int n_
 /* min and max of each slice (exact; order independent). */
 int udev_minmax(udev *d, const float *v, size_t n, int n_slices, float *host_min, float *host_max);
 
+/* ---- Streams and events for concurrent jobs ---- */
+int udev_stream_create(udev *d, void **s);
+void udev_stream_destroy(udev *d, void *s);
+/* Route all later work of this context to stream s (NULL = the context's own). */
+void udev_use_stream(udev *d, void *s);
+int udev_event_create(udev *d, void **e);
+void udev_event_destroy(void *e);
+int udev_event_record(udev *d, void *e);   /* on the current stream */
+/* 1 if the event's work has completed, 0 if not yet, < 0 on error. */
+int udev_event_done(udev *d, void *e);
+
 /* ---- Timing with CUDA events on the context's stream ---- */
 int udev_timer_begin(udev *d);
 int udev_timer_end(udev *d, float *ms);   /* waits for the stop event */

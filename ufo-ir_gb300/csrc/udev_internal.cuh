@@ -12,7 +12,8 @@ struct udev {
     int device = 0;
     int sm_count = 0;
     int smem_optin = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      /* where work goes now */
+    cudaStream_t own_stream = nullptr;  /* the context's own stream */
     char err[1024] = {0};
     uint64_t launches = 0;          /* kernels launched eagerly or through graphs */
     int capturing = 0;

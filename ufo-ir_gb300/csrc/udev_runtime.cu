@@ -67,12 +67,13 @@ int udev_create(int device, udev **out, char *err, size_t errlen)
     d->device = device;
     d->sm_count = prop.multiProcessorCount;
     d->smem_optin = (int) prop.sharedMemPerBlockOptin;
-    e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         snprintf(err, errlen, "cudaStreamCreate: %s", cudaGetErrorString(e));
         delete d;
         return UFOIR_ERR_CUDA;
     }
+    d->stream = d->own_stream;
     /* Keep freed stream-ordered memory in the pool instead of returning it to
      * the driver after every synchronisation. */
     cudaMemPool_t pool;
@@ -111,9 +112,65 @@ void udev_destroy(udev *d)
         cudaFree(d->d_err);
     if (d->h_err)
         cudaFreeHost(d->h_err);
-    if (d->stream)
-        cudaStreamDestroy(d->stream);
+    if (d->own_stream)
+        cudaStreamDestroy(d->own_stream);
     delete d;
+}
+
+int udev_stream_create(udev *d, void **s)
+{
+    UDEV_BIND(d);
+    cudaStream_t st = nullptr;
+    UDEV_CHECK(d, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    *s = (void *) st;
+    return UFOIR_OK;
+}
+
+void udev_stream_destroy(udev *d, void *s)
+{
+    if (!s)
+        return;
+    cudaSetDevice(d->device);
+    cudaStreamDestroy((cudaStream_t) s);
+}
+
+void udev_use_stream(udev *d, void *s)
+{
+    d->stream = s ? (cudaStream_t) s : d->own_stream;
+}
+
+int udev_event_create(udev *d, void **e)
+{
+    UDEV_BIND(d);
+    cudaEvent_t ev = nullptr;
+    UDEV_CHECK(d, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    *e = (void *) ev;
+    return UFOIR_OK;
+}
+
+void udev_event_destroy(void *e)
+{
+    if (e)
+        cudaEventDestroy((cudaEvent_t) e);
+}
+
+int udev_event_record(udev *d, void *e)
+{
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaEventRecord((cudaEvent_t) e, d->stream));
+    return UFOIR_OK;
+}
+
+int udev_event_done(udev *d, void *e)
+{
+    const cudaError_t r = cudaEventQuery((cudaEvent_t) e);
+    if (r == cudaSuccess)
+        return 1;
+    if (r == cudaErrorNotReady)
+        return 0;
+    cudaGetLastError();
+    udev_set_error(d, "event query: %s", cudaGetErrorString(r));
+    return UFOIR_ERR_CUDA;
 }
 
 int udev_device(const udev *d)
