@@ -275,6 +275,86 @@ UFOIR_API int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3]);
 UFOIR_API void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b);
 
 /* ------------------------------------------------------------------------ */
+/* Serving: a request loop over reconstruction jobs of mixed size, method   */
+/* and iteration count. The reference processes one slice per process()    */
+/* call on a ufo-core GPU node thread (src/core/ufo-ir-method-task.c:221-252) */
+/* and has no serving mode; this is the continuous-batching counterpart of  */
+/* calling ufoir_*_process once per job.                                    */
+/*                                                                          */
+/* A worker thread admits queued jobs in arrival order while the HBM budget */
+/* and the active-job limit allow, keeps each admitted job's sinogram and   */
+/* iterate resident on the device, and advances every active job a quantum */
+/* at a time on the job's own CUDA stream, so the work of different jobs    */
+/* overlaps on the GPU and a job is admitted as soon as memory frees up.    */
+/* Each job runs exactly the kernels of the plain call, so its result does  */
+/* not depend on what else is in flight. Policy ONE_AT_A_TIME admits one    */
+/* job at a time (the plain per-job path) for comparison.                   */
+/* ------------------------------------------------------------------------ */
+enum { UFOIR_METHOD_SART = 0, UFOIR_METHOD_SIRT = 1, UFOIR_METHOD_ASDPOCS = 2 };
+enum {
+    UFOIR_JOB_QUEUED = 0,
+    UFOIR_JOB_RUNNING = 1,
+    UFOIR_JOB_DONE = 2,
+    UFOIR_JOB_FAILED = 3,
+    UFOIR_JOB_CANCELLED = 4
+};
+enum { UFOIR_SERVE_CONTINUOUS = 0, UFOIR_SERVE_ONE_AT_A_TIME = 1 };
+
+typedef struct {
+    int method;                       /* UFOIR_METHOD_* */
+    unsigned int n_dets;              /* sinogram dims[0]; volume n_dets x n_dets */
+    unsigned int n_angles;            /* sinogram dims[1] */
+    float step;                       /* projector "step" */
+    float axis_position;              /* projector "axis_position" (-1 = centre) */
+    ufoir_sart_params sart;           /* SART and SIRT: num-iterations, relaxation_factor */
+    ufoir_asdpocs_params asdpocs;     /* ASD-POCS */
+} ufoir_job_desc;
+
+typedef struct {
+    uint64_t hbm_budget_bytes;        /* 0 = the context's budget */
+    unsigned int max_active_jobs;     /* 0 = 32 */
+    int policy;                       /* UFOIR_SERVE_* */
+    unsigned int quantum;             /* SIRT iterations / SART sweeps per scheduling turn; 0 = 1 */
+    unsigned int fail_allocation_every; /* testing: make every k-th job allocation fail (0 = off) */
+} ufoir_serve_config;
+
+typedef struct {
+    uint64_t submitted, completed, failed, cancelled, rejected;
+    double p50_latency_ms, p99_latency_ms, mean_latency_ms, max_latency_ms;
+    double p50_queue_ms, p99_queue_ms;
+    double throughput_jobs_per_s;     /* completed / (last completion - first submission) */
+    double busy_seconds;              /* first submission to last completion */
+    uint64_t peak_hbm_bytes;          /* largest sum of reserved job memory */
+    unsigned int peak_active_jobs;
+} ufoir_serve_stats;
+
+typedef struct ufoir_server ufoir_server;
+
+UFOIR_API void ufoir_serve_config_init(ufoir_serve_config *c);
+UFOIR_API void ufoir_job_desc_init(ufoir_job_desc *j);
+/* The server works on its own stream(s) on ctx's device and owns a worker
+ * thread; ctx must outlive it. */
+UFOIR_API int ufoir_serve_create(ufoir_ctx *ctx, const ufoir_serve_config *cfg, ufoir_server **out);
+/* Queue a job. sino (host memory, n_angles x n_dets floats) must stay valid
+ * until the job is admitted; vol (host memory, n_dets x n_dets floats)
+ * until it completes. Invalid parameters fail here (UFOIR_ERR_INVALID); a job
+ * larger than the whole budget is refused (UFOIR_ERR_BUDGET). */
+UFOIR_API int ufoir_serve_submit(ufoir_server *s, const ufoir_job_desc *job, const float *sino, float *vol,
+                                 uint64_t *job_id);
+UFOIR_API int ufoir_serve_poll(ufoir_server *s, uint64_t job_id, int *state);
+/* Wait up to timeout_ms (< 0 = forever) for the job to finish. Returns the
+ * job's own status (UFOIR_OK when done), UFOIR_ERR_CANCELLED, or
+ * UFOIR_ERR_TIMEOUT if it is still queued or running. */
+UFOIR_API int ufoir_serve_wait(ufoir_server *s, uint64_t job_id, int timeout_ms);
+/* Cancel a job that is still queued (running jobs finish). */
+UFOIR_API int ufoir_serve_cancel(ufoir_server *s, uint64_t job_id);
+/* Wait until every submitted job has finished (or timeout_ms passes). */
+UFOIR_API int ufoir_serve_drain(ufoir_server *s, int timeout_ms);
+UFOIR_API int ufoir_serve_get_stats(ufoir_server *s, ufoir_serve_stats *out);
+/* Cancels queued jobs, waits for running ones, stops the worker. */
+UFOIR_API void ufoir_serve_destroy(ufoir_server *s);
+
+/* ------------------------------------------------------------------------ */
 /* Reductions used by the methods, exposed for callers and tests.           */
 /* ufo_ir_op_l1_norm (src/core/ufo-ir-basic-ops.c:259-277) and              */
 /* ufo_ir_basic_ops_processor_dot_product (src/core/ufo-ir-basic-ops-processor.c:148-196, */

@@ -50,6 +50,58 @@ void ufoir__fp_scratch_free(ufoir_projector *p, ufoir_fp_scratch *s);
 /* Forward projection of all angles: out = (src + scale * A vol) [* w]. */
 int ufoir__fp_full(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, const float *src, const float *w,
                    int w_shared, float *out, float scale, int n_slices);
+/* Ray weights R = inv(FP(1)) (ones: n*n floats of scratch) and pixel weights
+ * C = inv(BP(1)) (ones: n_angles*n floats of scratch) for one slice. */
+int ufoir__ray_weights(ufoir_projector *p, float *R, float *ones);
+int ufoir__pixel_weights(ufoir_projector *p, float *C, float *ones);
+
+/* One SIRT iteration over n_slices slices (captured into graphs by callers). */
+typedef struct {
+    ufoir_projector *p;
+    udev_geom g;
+    const float *b;
+    float *x, *resid;
+    ufoir_fp_scratch fs;
+    const float *R, *C;
+    float lambda;
+    int n_slices;
+} ufoir__sirt_iter;
+int ufoir__sirt_body(void *arg);
+
+/* One SART sweep (every angle in order) over n_slices slices. */
+typedef struct {
+    ufoir_projector *p;
+    udev_geom g;
+    const float *b;
+    float *x, *resid;
+    const float *R;
+    float lambda;
+    int n_slices;
+} ufoir__sart_iter;
+int ufoir__sart_body(void *arg);
+
+/* ASD-POCS split into setup, one outer iteration and release, so that the
+ * plain call and the serve loop run the same code. */
+typedef struct {
+    ufoir_projector *p;
+    udev_geom g;
+    ufoir_asdpocs_params prm;
+    int S;
+    size_t n, na, nv, ns;
+    const float *b;
+    float *out;
+    float *x, *x_prev, *x_res, *b_res, *grad, *R;
+    ufoir_fp_scratch fs;
+    float *dp, *dd, *dg, *dtgv, *l1;    /* per-slice host scalars */
+    float beta, sart_relax;
+    unsigned int it;
+} ufoir__asd_state;
+int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *b,
+                     float *out, int S);
+int ufoir__asd_outer(ufoir__asd_state *s);
+void ufoir__asd_release(ufoir__asd_state *s);
+size_t ufoir__asd_bytes(size_t n, size_t na, size_t S);
+
 /* The two launches of ufoir__fp_full, separately (for timing). */
 int ufoir__fp_prepare(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, int n_slices);
 int ufoir__fp_project(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, const float *src, const float *w,

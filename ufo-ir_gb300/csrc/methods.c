@@ -91,7 +91,7 @@ static int check_relax(ufoir_ctx *ctx, float r)
 
 /* R = inv(FP(1)) over all angles for one slice (sirt-task.c:180-185,
  * sart-task.c:193-200). `ones` is scratch of n*n floats. */
-static int ray_weights(ufoir_projector *p, float *R, float *ones)
+int ufoir__ray_weights(ufoir_projector *p, float *R, float *ones)
 {
     ufoir_ctx *ctx = p->ctx;
     const size_t n = p->n_dets, nv = n * n, ns = n * p->n_angles;
@@ -111,7 +111,7 @@ static int ray_weights(ufoir_projector *p, float *R, float *ones)
 }
 
 /* C = inv(BP(1)) for one slice (sirt-task.c:188-193). `ones` holds ns floats. */
-static int pixel_weights(ufoir_projector *p, float *C, float *ones)
+int ufoir__pixel_weights(ufoir_projector *p, float *C, float *ones)
 {
     ufoir_ctx *ctx = p->ctx;
     udev_geom g;
@@ -168,20 +168,9 @@ static int run_graphed(ufoir_ctx *ctx, unsigned int iters, body_fn body, void *a
 /* ------------------------------------------------------------------------ */
 /* SIRT                                                                     */
 /* ------------------------------------------------------------------------ */
-typedef struct {
-    ufoir_projector *p;
-    udev_geom g;
-    const float *b;
-    float *x, *resid;
-    ufoir_fp_scratch fs;
-    const float *R, *C;
-    float lambda;
-    int n_slices;
-} sirt_iter;
-
-static int sirt_body(void *arg)
+int ufoir__sirt_body(void *arg)
 {
-    sirt_iter *s = (sirt_iter *) arg;
+    ufoir__sirt_iter *s = (ufoir__sirt_iter *) arg;
     udev *d = s->p->ctx->dev;
     /* sirt-task.c:202-213: r = (b - A x) * R;  x = x + C * (lambda A^T r) */
     int rc = ufoir__fp_full(s->p, &s->fs, s->x, s->b, s->R, 1, s->resid, -1.0f, s->n_slices);
@@ -206,7 +195,7 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
     const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
     ufoir_buf bb = {0}, bx = {0};
     float *R = NULL, *C = NULL, *resid = NULL;
-    sirt_iter it;
+    ufoir__sirt_iter it;
     memset(&it, 0, sizeof(it));
     UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
@@ -219,8 +208,8 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
      * the output volume serves as the all-ones image before it is zeroed */
     proj->prm.relaxation = 1.0f;
     proj->prm.correction_scale = 1.0f;
-    UFOIR_TRY(ray_weights(proj, R, bx.dev));
-    UFOIR_TRY(pixel_weights(proj, C, resid));
+    UFOIR_TRY(ufoir__ray_weights(proj, R, bx.dev));
+    UFOIR_TRY(ufoir__pixel_weights(proj, C, resid));
     proj->prm.relaxation = prm->relaxation_factor;
     proj->prm.correction_scale = -1.0f;
     UFOIR_TRY(udev_fill(ctx->dev, bx.dev, nv * n_slices, 0.0f));
@@ -234,7 +223,7 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
     it.C = C;
     it.lambda = prm->relaxation_factor;
     it.n_slices = (int) n_slices;
-    UFOIR_TRY(run_graphed(ctx, prm->num_iterations, sirt_body, &it));
+    UFOIR_TRY(run_graphed(ctx, prm->num_iterations, ufoir__sirt_body, &it));
     UFOIR_TRY(udev_take_kernel_error(ctx->dev));
     UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
 done:
@@ -256,7 +245,7 @@ done:
 /* ------------------------------------------------------------------------ */
 struct ufoir_sirt_batch {
     ufoir_projector *proj;
-    sirt_iter it;
+    ufoir__sirt_iter it;
     float *R, *C, *resid;
     size_t nv;
     void *exec;
@@ -305,8 +294,8 @@ int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *prm,
     UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &b->it.fs, n_slices));
     proj->prm.relaxation = 1.0f;
     proj->prm.correction_scale = 1.0f;
-    UFOIR_TRY(ray_weights(proj, b->R, d_vol));
-    UFOIR_TRY(pixel_weights(proj, b->C, b->resid));
+    UFOIR_TRY(ufoir__ray_weights(proj, b->R, d_vol));
+    UFOIR_TRY(ufoir__pixel_weights(proj, b->C, b->resid));
     proj->prm.relaxation = prm->relaxation_factor;
     proj->prm.correction_scale = -1.0f;
     UFOIR_TRY(udev_fill(ctx->dev, d_vol, nv * n_slices, 0.0f));
@@ -320,7 +309,7 @@ int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *prm,
     b->it.lambda = prm->relaxation_factor;
     b->it.n_slices = (int) n_slices;
     UFOIR_TRY(udev_capture_begin(ctx->dev));
-    rc = sirt_body(&b->it);
+    rc = ufoir__sirt_body(&b->it);
     {
         const int rc2 = udev_capture_end(ctx->dev, &b->exec, &b->exec_kernels);
         if (!rc)
@@ -362,7 +351,7 @@ int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3])
 {
     if (!b || !ms)
         return UFOIR_ERR_INVALID;
-    sirt_iter *s = &b->it;
+    ufoir__sirt_iter *s = &b->it;
     udev *d = s->p->ctx->dev;
     int rc;
     if ((rc = udev_timer_begin(d)) || (rc = ufoir__fp_prepare(s->p, &s->fs, s->x, s->n_slices)) ||
@@ -383,19 +372,9 @@ int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3])
 /* ------------------------------------------------------------------------ */
 /* SART                                                                     */
 /* ------------------------------------------------------------------------ */
-typedef struct {
-    ufoir_projector *p;
-    udev_geom g;
-    const float *b;
-    float *x, *resid;
-    const float *R;
-    float lambda;
-    int n_slices;
-} sart_iter;
-
-static int sart_body(void *arg)
+int ufoir__sart_body(void *arg)
 {
-    sart_iter *s = (sart_iter *) arg;
+    ufoir__sart_iter *s = (ufoir__sart_iter *) arg;
     udev *d = s->p->ctx->dev;
     int rc = UFOIR_OK;
     /* sart-task.c:209-217: per angle, r_theta = (b_theta - A_theta x) * R_theta;
@@ -424,7 +403,7 @@ static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, con
     int rc = udev_fill(ctx->dev, x, nv * (size_t) n_slices, 0.0f);
     if (rc)
         return rc;
-    sart_iter it;
+    ufoir__sart_iter it;
     it.p = proj;
     ufoir__projector_geom(proj, &it.g);
     it.b = b;
@@ -440,7 +419,7 @@ static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, con
     rc = udev_capture_begin(ctx->dev);
     if (rc)
         return rc;
-    rc = sart_body(&it);
+    rc = ufoir__sart_body(&it);
     rc2 = udev_capture_end(ctx->dev, &exec, &kernels);
     if (rc || rc2) {
         udev_graph_destroy(exec);
@@ -474,7 +453,7 @@ int ufoir_sart_process(ufoir_projector *proj, const ufoir_sart_params *prm, cons
     UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices > nv ? ns * n_slices : nv));
     proj->prm.correction_scale = 1.0f;
-    UFOIR_TRY(ray_weights(proj, R, resid));
+    UFOIR_TRY(ufoir__ray_weights(proj, R, resid));
     UFOIR_TRY(sart_run(proj, prm->num_iterations, prm->relaxation_factor, bb.dev, bx.dev, resid, R,
                        (int) n_slices));
     UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
@@ -490,12 +469,8 @@ done:
 /* ------------------------------------------------------------------------ */
 /* ASD-POCS                                                                 */
 /* ------------------------------------------------------------------------ */
-int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
-                          const size_t dims[2], float *vol, size_t n_slices)
+static int asdpocs_check(ufoir_ctx *ctx, const ufoir_asdpocs_params *prm)
 {
-    if (!proj || !prm || !sino || !vol || !dims)
-        return UFOIR_ERR_INVALID;
-    ufoir_ctx *ctx = proj->ctx;
     int rc;
     if (prm->df_minimizer.num_iterations < 1)
         return ufoir__fail(ctx, UFOIR_ERR_INVALID, "df_minimizer num-iterations must be >= 1");
@@ -507,105 +482,168 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
         return ufoir__fail(ctx, UFOIR_ERR_INVALID, "ng %u outside [0, 1000]", prm->ng);
     if (prm->norm_mode != UFOIR_NORM_COMPAT && prm->norm_mode != UFOIR_NORM_FP64)
         return ufoir__fail(ctx, UFOIR_ERR_INVALID, "unknown norm_mode %d", prm->norm_mode);
-    rc = method_setup(proj, dims, n_slices, prm->num_iterations);
-    if (rc)
-        return rc;
-    const size_t n = proj->n_dets, na = proj->n_angles, nv = n * n, ns = n * na;
-    const int S = (int) n_slices;
-    udev *d = ctx->dev;
-    udev_geom g;
-    ufoir__projector_geom(proj, &g);
-    ufoir_buf bb = {0}, bo = {0};
-    float *x = NULL, *x_prev = NULL, *x_res = NULL, *b_res = NULL, *grad = NULL, *R = NULL;
-    ufoir_fp_scratch fs = {NULL, NULL, 0};
-    float *dp = NULL, *dd = NULL, *dg = NULL, *dtgv = NULL, *l1 = NULL;
-    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
-    UFOIR_TRY(ufoir__buf_in(ctx, &bo, vol, nv * n_slices, 0));
-    UFOIR_TRY(ufoir__alloc(ctx, &x, nv * n_slices));
-    UFOIR_TRY(ufoir__alloc(ctx, &x_prev, nv * n_slices));
-    UFOIR_TRY(ufoir__alloc(ctx, &x_res, nv * n_slices));
-    UFOIR_TRY(ufoir__alloc(ctx, &b_res, ns * n_slices > nv ? ns * n_slices : nv));
-    UFOIR_TRY(ufoir__alloc(ctx, &grad, nv * n_slices));
-    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &fs, n_slices));
-    UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
-    dp = (float *) calloc((size_t) S * 5, sizeof(float));
-    if (!dp) {
+    if (prm->num_iterations < 1)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "num-iterations must be >= 1");
+    return UFOIR_OK;
+}
+
+void ufoir__asd_release(ufoir__asd_state *s)
+{
+    ufoir_ctx *ctx = s->p->ctx;
+    free(s->dp);
+    s->dp = NULL;
+    ufoir__free(ctx, s->x);
+    ufoir__free(ctx, s->x_prev);
+    ufoir__free(ctx, s->x_res);
+    ufoir__free(ctx, s->b_res);
+    ufoir__free(ctx, s->grad);
+    ufoir__free(ctx, s->R);
+    ufoir__fp_scratch_free(s->p, &s->fs);
+    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = NULL;
+}
+
+size_t ufoir__asd_bytes(size_t n, size_t na, size_t S)
+{
+    const size_t nv = n * n, ns = n * na, pitch = (size_t) udev_fp_pitch((int) n);
+    const size_t bres = ns * S > nv ? ns * S : nv;
+    return sizeof(float) * (4 * nv * S + bres + ns + 2 * n * pitch * S);
+}
+
+/* Buffers, weights and the first state of asdpocs-task.c:411-455. The
+ * geometry must be prepared; b and out are device memory (S slices). */
+int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *b,
+                     float *out, int S)
+{
+    ufoir_ctx *ctx = proj->ctx;
+    memset(s, 0, sizeof(*s));
+    s->p = proj;
+    s->prm = *prm;
+    s->S = S;
+    s->n = proj->n_dets;
+    s->na = proj->n_angles;
+    s->nv = s->n * s->n;
+    s->ns = s->n * s->na;
+    s->b = b;
+    s->out = out;
+    ufoir__projector_geom(proj, &s->g);
+    const size_t nv = s->nv, ns = s->ns;
+    int rc;
+    UFOIR_TRY(ufoir__alloc(ctx, &s->x, nv * S));
+    UFOIR_TRY(ufoir__alloc(ctx, &s->x_prev, nv * S));
+    UFOIR_TRY(ufoir__alloc(ctx, &s->x_res, nv * S));
+    UFOIR_TRY(ufoir__alloc(ctx, &s->b_res, ns * S > nv ? ns * S : nv));
+    UFOIR_TRY(ufoir__alloc(ctx, &s->grad, nv * S));
+    UFOIR_TRY(ufoir__alloc(ctx, &s->R, ns));
+    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &s->fs, (size_t) S));
+    s->dp = (float *) calloc((size_t) S * 5, sizeof(float));
+    if (!s->dp) {
         rc = ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
         goto done;
     }
-    dd = dp + S;
-    dg = dd + S;
-    dtgv = dg + S;
-    l1 = dtgv + S;
-    for (int s = 0; s < S; s++)
-        dp[s] = dd[s] = dg[s] = dtgv[s] = 1.0f;
-
-    UFOIR_TRY(udev_fill(d, x, nv * n_slices, 0.0f));
-    UFOIR_TRY(udev_fill(d, x_prev, nv * n_slices, 0.0f));
+    s->dd = s->dp + S;
+    s->dg = s->dd + S;
+    s->dtgv = s->dg + S;
+    s->l1 = s->dtgv + S;
+    for (int i = 0; i < S; i++)
+        s->dp[i] = s->dd[i] = s->dg[i] = s->dtgv[i] = 1.0f;
+    UFOIR_TRY(udev_fill(ctx->dev, s->x, nv * S, 0.0f));
+    UFOIR_TRY(udev_fill(ctx->dev, s->x_prev, nv * S, 0.0f));
     /* SART's ray weights depend on the geometry only; the reference
      * recomputes the same values on every df_minimizer call. */
     proj->prm.correction_scale = 1.0f;
-    UFOIR_TRY(ray_weights(proj, R, b_res));
+    UFOIR_TRY(ufoir__ray_weights(proj, s->R, s->b_res));
+    s->beta = prm->beta;
+    s->sart_relax = prm->df_minimizer.relaxation_factor;
+    s->it = 0;
+    return UFOIR_OK;
+done:
+    ufoir__asd_release(s);
+    return rc;
+}
 
-    float beta = prm->beta;
-    float sart_relax = prm->df_minimizer.relaxation_factor;
-    for (unsigned int it = 0; it < prm->num_iterations; it++) {
-        /* g_object_set(df_minimizer, "relaxation_factor", beta) (:459); the
-         * property's range is [0, 1] and GObject rejects values outside it. */
-        if (beta >= 0.0f && beta <= 1.0f)
-            sart_relax = beta;
-        UFOIR_TRY(sart_run(proj, prm->df_minimizer.num_iterations, sart_relax, bb.dev, x, b_res, R, S));
-
-        if (prm->positive_constraint)
-            UFOIR_TRY(udev_unary(d, UDEV_POSC, x, 0, 0, x, nv * n_slices));
-
-        UFOIR_TRY(udev_memcpy_async(d, bo.dev, x, nv * n_slices * sizeof(float)));
-
-        /* b_res = b - A x (:470-475) */
-        proj->prm.correction_scale = -1.0f;
-        UFOIR_TRY(ufoir__fp_full(proj, &fs, x, bb.dev, NULL, 0, b_res, -1.0f, S));
-        UFOIR_TRY(udev_l1_norm(d, b_res, n, na, S, prm->norm_mode, dd));
-
-        UFOIR_TRY(udev_binary(d, UDEV_SUB, x, x_prev, 0, x_res, nv * n_slices));
-        UFOIR_TRY(udev_l1_norm(d, x_res, n, n, S, prm->norm_mode, dp));
-
-        if (it == 0)
-            for (int s = 0; s < S; s++)
-                dtgv[s] = prm->alpha * dp[s];
-
-        UFOIR_TRY(udev_memcpy_async(d, x_prev, x, nv * n_slices * sizeof(float)));
-
-        /* ufo_math_tvstd_method_process_real (:550-580): 20 sub-steps */
-        for (int step = 0; step < 20; step++) {
-            UFOIR_TRY(udev_l1_grad(d, x, grad, (int) n, (int) n, S));
-            UFOIR_TRY(udev_l1_norm(d, grad, n, n, S, prm->norm_mode, l1));
-            for (int s = 0; s < S; s++) {
-                const float factor = dtgv[s] / l1[s];
-                UFOIR_TRY(udev_binary(d, UDEV_SUB_SCALED, x + (size_t) s * nv, grad + (size_t) s * nv, factor,
-                                      x + (size_t) s * nv, nv));
-            }
+/* One outer iteration of asdpocs-task.c:457-506 (synchronous: the norms
+ * come back to the host for the reference's float scalar logic). */
+int ufoir__asd_outer(ufoir__asd_state *s)
+{
+    ufoir_projector *proj = s->p;
+    udev *d = proj->ctx->dev;
+    const size_t n = s->n, na = s->na, nv = s->nv;
+    const int S = s->S;
+    const ufoir_asdpocs_params *prm = &s->prm;
+    int rc;
+    /* g_object_set(df_minimizer, "relaxation_factor", beta) (:459); the
+     * property's range is [0, 1] and GObject rejects values outside it. */
+    if (s->beta >= 0.0f && s->beta <= 1.0f)
+        s->sart_relax = s->beta;
+    if ((rc = sart_run(proj, prm->df_minimizer.num_iterations, s->sart_relax, s->b, s->x, s->b_res, s->R, S)))
+        return rc;
+    if (prm->positive_constraint && (rc = udev_unary(d, UDEV_POSC, s->x, 0, 0, s->x, nv * S)))
+        return rc;
+    if ((rc = udev_memcpy_async(d, s->out, s->x, nv * S * sizeof(float))))
+        return rc;
+    /* b_res = b - A x (:470-475) */
+    proj->prm.correction_scale = -1.0f;
+    if ((rc = ufoir__fp_full(proj, &s->fs, s->x, s->b, NULL, 0, s->b_res, -1.0f, S)) ||
+        (rc = udev_l1_norm(d, s->b_res, n, na, S, prm->norm_mode, s->dd)) ||
+        (rc = udev_binary(d, UDEV_SUB, s->x, s->x_prev, 0, s->x_res, nv * S)) ||
+        (rc = udev_l1_norm(d, s->x_res, n, n, S, prm->norm_mode, s->dp)))
+        return rc;
+    if (s->it == 0)
+        for (int i = 0; i < S; i++)
+            s->dtgv[i] = prm->alpha * s->dp[i];
+    if ((rc = udev_memcpy_async(d, s->x_prev, s->x, nv * S * sizeof(float))))
+        return rc;
+    /* ufo_math_tvstd_method_process_real (:550-580): 20 sub-steps */
+    for (int step = 0; step < 20; step++) {
+        if ((rc = udev_l1_grad(d, s->x, s->grad, (int) n, (int) n, S)) ||
+            (rc = udev_l1_norm(d, s->grad, n, n, S, prm->norm_mode, s->l1)))
+            return rc;
+        for (int i = 0; i < S; i++) {
+            const float factor = s->dtgv[i] / s->l1[i];
+            if ((rc = udev_binary(d, UDEV_SUB_SCALED, s->x + (size_t) i * nv, s->grad + (size_t) i * nv, factor,
+                                  s->x + (size_t) i * nv, nv)))
+                return rc;
         }
-
-        UFOIR_TRY(udev_binary(d, UDEV_SUB, x, x_prev, 0, x_res, nv * n_slices));
-        UFOIR_TRY(udev_l1_norm(d, x_res, n, n, S, prm->norm_mode, dg));
-        beta *= prm->beta_red;
-        for (int s = 0; s < S; s++)
-            if (dg[s] > prm->r_max * dp[s] && dd[s] > 0.001f)
-                dtgv[s] *= prm->alpha_red;
     }
+    if ((rc = udev_binary(d, UDEV_SUB, s->x, s->x_prev, 0, s->x_res, nv * S)) ||
+        (rc = udev_l1_norm(d, s->x_res, n, n, S, prm->norm_mode, s->dg)))
+        return rc;
+    s->beta *= prm->beta_red;
+    for (int i = 0; i < S; i++)
+        if (s->dg[i] > prm->r_max * s->dp[i] && s->dd[i] > 0.001f)
+            s->dtgv[i] *= prm->alpha_red;
+    s->it++;
+    return UFOIR_OK;
+}
+
+int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
+                          const size_t dims[2], float *vol, size_t n_slices)
+{
+    if (!proj || !prm || !sino || !vol || !dims)
+        return UFOIR_ERR_INVALID;
+    ufoir_ctx *ctx = proj->ctx;
+    int rc = asdpocs_check(ctx, prm);
+    if (rc)
+        return rc;
+    rc = method_setup(proj, dims, n_slices, prm->num_iterations);
+    if (rc)
+        return rc;
+    const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    ufoir_buf bb = {0}, bo = {0};
+    ufoir__asd_state st;
+    memset(&st, 0, sizeof(st));
+    st.p = proj;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bo, vol, nv * n_slices, 0));
+    UFOIR_TRY(ufoir__asd_setup(&st, proj, prm, bb.dev, bo.dev, (int) n_slices));
+    for (unsigned int it = 0; it < prm->num_iterations; it++)
+        UFOIR_TRY(ufoir__asd_outer(&st));
     UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
 done:
-    free(dp);
-    ufoir__free(ctx, x);
-    ufoir__free(ctx, x_prev);
-    ufoir__free(ctx, x_res);
-    ufoir__free(ctx, b_res);
-    ufoir__free(ctx, grad);
-    ufoir__fp_scratch_free(proj, &fs);
-    ufoir__free(ctx, R);
+    ufoir__asd_release(&st);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bo);
-    udev_sync(d);
+    udev_sync(ctx->dev);
     return rc;
 }
 

@@ -72,6 +72,36 @@ class SbtvParams(C.Structure):
                 ("norm_mode", C.c_int)]
 
 
+METHOD_SART = 0
+METHOD_SIRT = 1
+METHOD_ASDPOCS = 2
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = 0, 1, 2, 3, 4
+SERVE_CONTINUOUS = 0
+SERVE_ONE_AT_A_TIME = 1
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("method", C.c_int), ("n_dets", C.c_uint), ("n_angles", C.c_uint), ("step", C.c_float),
+                ("axis_position", C.c_float), ("sart", SartParams), ("asdpocs", AsdpocsParams)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_uint), ("policy", C.c_int),
+                ("quantum", C.c_uint), ("fail_allocation_every", C.c_uint)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("rejected", C.c_uint64), ("p50_latency_ms", C.c_double),
+                ("p99_latency_ms", C.c_double), ("mean_latency_ms", C.c_double), ("max_latency_ms", C.c_double),
+                ("p50_queue_ms", C.c_double), ("p99_queue_ms", C.c_double),
+                ("throughput_jobs_per_s", C.c_double), ("busy_seconds", C.c_double),
+                ("peak_hbm_bytes", C.c_uint64), ("peak_active_jobs", C.c_uint)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 # Every symbol include/ufoir.h declares (checked by the CPU test suite).
@@ -89,7 +119,9 @@ EXPORTED = (
     "ufoir_sbtv_process", "ufoir_l1_norm", "ufoir_dot_product",
     "ufoir_sirt_batch_create", "ufoir_sirt_batch_run", "ufoir_sirt_batch_reset",
     "ufoir_sirt_batch_profile", "ufoir_sirt_batch_destroy", "ufoir_ctx_timer_begin",
-    "ufoir_ctx_timer_end",
+    "ufoir_ctx_timer_end", "ufoir_serve_config_init", "ufoir_job_desc_init", "ufoir_serve_create",
+    "ufoir_serve_submit", "ufoir_serve_poll", "ufoir_serve_wait", "ufoir_serve_cancel", "ufoir_serve_drain",
+    "ufoir_serve_get_stats", "ufoir_serve_destroy",
 )
 
 
@@ -154,6 +186,19 @@ def _declare(L):
     L.ufoir_sirt_batch_profile.argtypes = [vp, f32p]
     L.ufoir_sirt_batch_destroy.argtypes = [vp]
     L.ufoir_sirt_batch_destroy.restype = None
+    L.ufoir_serve_config_init.argtypes = [C.POINTER(ServeConfig)]
+    L.ufoir_serve_config_init.restype = None
+    L.ufoir_job_desc_init.argtypes = [C.POINTER(JobDesc)]
+    L.ufoir_job_desc_init.restype = None
+    L.ufoir_serve_create.argtypes = [vp, C.POINTER(ServeConfig), C.POINTER(vp)]
+    L.ufoir_serve_submit.argtypes = [vp, C.POINTER(JobDesc), vp, vp, C.POINTER(C.c_uint64)]
+    L.ufoir_serve_poll.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int)]
+    L.ufoir_serve_wait.argtypes = [vp, C.c_uint64, C.c_int]
+    L.ufoir_serve_cancel.argtypes = [vp, C.c_uint64]
+    L.ufoir_serve_drain.argtypes = [vp, C.c_int]
+    L.ufoir_serve_get_stats.argtypes = [vp, C.POINTER(ServeStats)]
+    L.ufoir_serve_destroy.argtypes = [vp]
+    L.ufoir_serve_destroy.restype = None
     L.ufoir_l1_norm.argtypes = [vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
     L.ufoir_dot_product.argtypes = [vp, vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
 
@@ -473,3 +518,79 @@ def asdpocs(proj, sino, vol=None, **kw):
 
 def sbtv(proj, sino, vol=None, **kw):
     return _run_method("sbtv", proj, sbtv_params(**kw), sino, vol)
+
+
+def job_desc(method, n_dets, n_angles, step, axis_position=-1.0, **kw) -> JobDesc:
+    """A reconstruction job. kw: num_iterations / relaxation_factor (SART, SIRT)
+    or asdpocs=dict(...) (ASD-POCS parameters, with df_minimizer=dict(...))."""
+    j = JobDesc()
+    lib().ufoir_job_desc_init(C.byref(j))
+    j.method, j.n_dets, j.n_angles, j.step, j.axis_position = method, n_dets, n_angles, step, axis_position
+    if "asdpocs" in kw:
+        j.asdpocs = asdpocs_params(**kw.pop("asdpocs"))
+    if kw:
+        j.sart = sart_params(**kw)
+    return j
+
+
+class Server:
+    """The continuous-batching request loop (ufoir_serve_*)."""
+
+    def __init__(self, ctx: Context, hbm_budget: int = 0, max_active_jobs: int = 0,
+                 policy: int = SERVE_CONTINUOUS, quantum: int = 1, fail_allocation_every: int = 0):
+        self.ctx = ctx
+        cfg = ServeConfig()
+        lib().ufoir_serve_config_init(C.byref(cfg))
+        cfg.hbm_budget_bytes = hbm_budget
+        if max_active_jobs:
+            cfg.max_active_jobs = max_active_jobs
+        cfg.policy = policy
+        cfg.quantum = quantum
+        cfg.fail_allocation_every = fail_allocation_every
+        h = C.c_void_p()
+        ctx._check(lib().ufoir_serve_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+        self._keep = {}
+
+    def submit(self, job: JobDesc, sino: np.ndarray, vol: np.ndarray = None):
+        """Queue a job; returns (job_id, output array). Arrays must stay alive until done."""
+        if vol is None:
+            vol = np.zeros((job.n_dets, job.n_dets), np.float32)
+        assert sino.dtype == np.float32 and sino.flags.c_contiguous and sino.size == job.n_dets * job.n_angles
+        jid = C.c_uint64()
+        rc = lib().ufoir_serve_submit(self.handle, C.byref(job), sino.ctypes.data, vol.ctypes.data, C.byref(jid))
+        if rc != OK:
+            raise UfoirError(rc, self.ctx.last_error())
+        self._keep[jid.value] = (sino, vol)
+        return jid.value, vol
+
+    def poll(self, jid: int) -> int:
+        st = C.c_int()
+        self.ctx._check(lib().ufoir_serve_poll(self.handle, jid, C.byref(st)))
+        return st.value
+
+    def wait(self, jid: int, timeout_ms: int = -1) -> int:
+        return lib().ufoir_serve_wait(self.handle, jid, timeout_ms)
+
+    def cancel(self, jid: int) -> int:
+        return lib().ufoir_serve_cancel(self.handle, jid)
+
+    def drain(self, timeout_ms: int = -1) -> int:
+        return lib().ufoir_serve_drain(self.handle, timeout_ms)
+
+    def stats(self) -> dict:
+        s = ServeStats()
+        self.ctx._check(lib().ufoir_serve_get_stats(self.handle, C.byref(s)))
+        return s.as_dict()
+
+    def close(self):
+        if self.handle:
+            lib().ufoir_serve_destroy(self.handle)
+            self.handle = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
