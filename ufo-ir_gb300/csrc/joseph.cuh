@@ -17,6 +17,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 namespace joseph {
 
 /* Per-geometry constants shared by FP and BP (…joseph.cl:51-60, :174-187). */
@@ -93,6 +95,132 @@ __device__ __forceinline__ void lerp_coord(float c, int &i0, float &t)
 __device__ __forceinline__ float lerp(float t, float t0, float t1)
 {
     return __fadd_rn(__fmul_rn(__fsub_rn(1.0f, t), t0), __fmul_rn(t, t1));
+}
+
+/* 32-bit shared-memory load. */
+__device__ __forceinline__ float lds(uint32_t addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
+/* floor() by a round-toward-minus-infinity add of 1.5 * 2^23: for
+ * |x| < 2^22, y = x + M lands in [2^23, 2^24) where floats are integers, so
+ * y - M == floor(x) exactly and the bits of y are floor(x) + kFloorMagicBits. */
+constexpr float kFloorMagic = 12582912.0f;
+constexpr int kFloorMagicBits = 0x4B400000;
+
+/* One exact linear-filter tap pair read from shared memory: row_base is the
+ * 32-bit shared address of element 0 of the row, minus 4 * kFloorMagicBits. */
+__device__ __forceinline__ float sample_smem(float c, uint32_t row_base)
+{
+    const float cm = __fsub_rn(c, 0.5f);
+    const float y = __fadd_rd(cm, kFloorMagic);
+    const float fi = __fsub_rn(y, kFloorMagic);
+    const float t = __fsub_rn(cm, fi);
+    const uint32_t addr = row_base + 4u * (uint32_t) __float_as_int(y);
+    return lerp(t, lds(addr), lds(addr + 4u));
+}
+
+/*
+ * Paired forms for two samples at once, on the packed FP32 instructions of
+ * sm_100 and later (PTX add/sub/mul/fma .f32x2). Each lane rounds exactly as
+ * the scalar instruction. The code generator fuses a packed multiply that
+ * feeds a packed add into one fused multiply-add even with explicit rounding
+ * modifiers, which changes the rounding, so every product that is added
+ * later is written as fma(a, b, z) with z = -0.0 supplied at run time (the
+ * compiler cannot fold it): a*b + (-0) rounds exactly as a*b, signed zeros
+ * included, and an fma cannot be fused further.
+ */
+__device__ __forceinline__ unsigned long long pack2(float2 a)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 unpack2(unsigned long long r)
+{
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+
+__device__ __forceinline__ float2 splat(float a)
+{
+    return make_float2(a, a);
+}
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+
+/* round toward minus infinity */
+__device__ __forceinline__ float2 add2_rd(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("add.rm.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+
+/* a * b, for products that are not added afterwards */
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+
+/* a * b as fma(a, b, z), z = (-0, -0) from a run-time value: a product that
+ * can be added to something else without being fused into it. */
+__device__ __forceinline__ float2 mul2z(float2 a, float2 b, float2 z)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)), "l"(pack2(z)));
+    return unpack2(r);
+}
+
+/* (1 - t) * T0 + t * T1 per lane, each operation rounded. */
+__device__ __forceinline__ float2 lerp2(float2 t, float2 t0, float2 t1, float2 z)
+{
+    return add2(mul2z(sub2(splat(1.0f), t), t0, z), mul2z(t, t1, z));
+}
+
+/*
+ * floor(c - 0.5) and t = (c - 0.5) - floor(c - 0.5) for coordinates c >= 0.5,
+ * in three paired operations: y = rd(c + (2^23 - 0.5)) lands in [2^23, 2^24)
+ * with bits kHalfFloorBits + floor(c - 0.5); y - (2^23 - 0.5) and c minus it
+ * are exact, and c - 0.5 itself is exact for c >= 0.5, so t is the same
+ * fraction the four-step form computes.
+ */
+constexpr float kHalfFloorMagic = 8388607.5f;
+constexpr int kHalfFloorBits = 0x4B000000;
+
+__device__ __forceinline__ float2 floor_half2(float2 c, float2 &t)
+{
+    const float2 y = add2_rd(c, splat(kHalfFloorMagic));
+    t = sub2(c, sub2(y, splat(kHalfFloorMagic)));
+    return y;
+}
+
+/* The same for any |c - 0.5| < 2^22 (bits kFloorMagicBits + floor(c - 0.5)). */
+__device__ __forceinline__ float2 floor_any2(float2 c, float2 &t)
+{
+    const float2 cm = sub2(c, splat(0.5f));
+    const float2 y = add2_rd(cm, splat(kFloorMagic));
+    t = sub2(cm, sub2(y, splat(kFloorMagic)));
+    return y;
 }
 
 /* Bounds-checked texel of a row with a zero border. */

@@ -2,9 +2,9 @@
  * udev_bp_tiles.cu - pixel-driven backprojection over many angles, with the
  * sinogram windows of a pixel tile staged in shared memory.
  *
- * One CTA owns a 32 x 32 pixel tile; thread (tx, ty) owns the 4 pixels
- * (x0 + tx, y0 + ty + 8p), p < 4, which share fX * cos(theta). For a chunk of
- * 32 angles the CTA copies, per angle, the 64 detector values that the tile
+ * One CTA owns a 32 x 64 pixel tile; thread (tx, ty) owns the 8 pixels
+ * (x0 + tx, y0 + ty + 8p), p < 8, which share fX * cos(theta). For a chunk of
+ * 32 angles the CTA copies, per angle, the 128 detector values that the tile
  * can reach (cp.async, double buffered; detectors outside [0, n) read 0),
  * so every sample reads shared memory and a warp's 32 lanes (adjacent x)
  * touch adjacent words.
@@ -24,13 +24,14 @@ namespace {
 
 constexpr int kTX = 32;
 constexpr int kTY = 8;
-constexpr int kPY = 4;               /* pixels per thread (one column) */
-constexpr int kTile = kTX;           /* tile is kTile x kTile pixels */
+constexpr int kPY = 8;               /* pixels per thread (one column) */
+constexpr int kTileX = kTX;          /* tile is kTileX x kTileY pixels */
+constexpr int kTileY = kTY * kPY;
 constexpr int kAC = 32;              /* angles per chunk */
-constexpr int kWin = 64;             /* detector window per angle */
+constexpr int kWin = 128;            /* detector window per angle (tile span <= 71) */
 constexpr int kMaxSub = 16;
-constexpr float kFloorMagic = 12582912.0f;
-constexpr int kFloorMagicBits = 0x4B400000;
+
+
 
 struct BpTileArgs {
     const float *sino;
@@ -48,20 +49,30 @@ struct BpTileArgs {
     long long cw_stride;
     int n_subsets;
     int total_angles;
+    int contiguous;      /* subsets cover [first_angle, first_angle + total) in order */
+    int first_angle;
+    float neg_zero;      /* -0.0f: the addend of unfusable packed products */
     unsigned int sub_offset[kMaxSub];
     unsigned int sub_n[kMaxSub];
 };
 
+/* Per angle of a chunk: cos, sin, and the first detector of its window
+ * (as int bits); one 16-byte shared load. */
 struct __align__(16) BpSmem {
     float win[2][kAC][kWin];
-    float cs[2][kAC];
-    float sn[2][kAC];
-    int w0[2][kAC];
+    float4 ang[2][kAC];
 };
 
 __device__ __forceinline__ void cp_async4(float *dst, const float *src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t) __cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(float *dst, const float *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t) __cvta_generic_to_shared(dst)),
                  "l"(src)
                  : "memory");
 }
@@ -80,6 +91,8 @@ __device__ __forceinline__ void cp_async_wait()
 /* Angle of virtual index vi (angles of the subsets, in order). */
 __device__ __forceinline__ int angle_of(const BpTileArgs &P, int vi)
 {
+    if (P.contiguous)
+        return P.first_angle + vi;
     for (int k = 0; k < P.n_subsets; ++k) {
         if (vi < (int) P.sub_n[k])
             return (int) P.sub_offset[k] + vi;
@@ -94,74 +107,103 @@ __device__ __forceinline__ float det_coord(float fX, float fY, float cs, float s
     return __fadd_rn(__fsub_rn(__fmul_rn(fX, cs), __fmul_rn(fY, sn)), shift);
 }
 
+/*
+ * Stages the windows of one chunk of angles. Each window starts at a detector
+ * whose global address is 16-byte aligned, at most 3 before the leftmost
+ * reachable tap, so the bulk of it moves in 16-byte cp.async copies; groups
+ * that cross the ends of the detector row go element by element, with zeros
+ * outside [0, n).
+ */
 __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, const float *sino, int x0, int y0,
                            const joseph::AxisConsts &k, float e0, float e1, float shift)
 {
     const int tid = threadIdx.y * kTX + threadIdx.x;
     const int first = chunk * kAC;
     const int count = min(kAC, P.total_angles - first);
-    /* one thread per angle: LUT values and window start */
     if (tid < count) {
         const int a = angle_of(P, first + tid);
         const float cs = __ldg(P.cosv + a), sn = __ldg(P.sinv + a);
-        S.cs[buf][tid] = cs;
-        S.sn[buf][tid] = sn;
         const float fx0 = __fsub_rn(__fadd_rn((float) x0, 0.5f), k.os);
-        const float fx1 = __fsub_rn(__fadd_rn((float) (x0 + kTile - 1), 0.5f), k.os);
+        const float fx1 = __fsub_rn(__fadd_rn((float) (x0 + kTileX - 1), 0.5f), k.os);
         const float fy0 = __fsub_rn(__fadd_rn((float) y0, 0.5f), k.os);
-        const float fy1 = __fsub_rn(__fadd_rn((float) (y0 + kTile - 1), 0.5f), k.os);
+        const float fy1 = __fsub_rn(__fadd_rn((float) (y0 + kTileY - 1), 0.5f), k.os);
         const float c00 = det_coord(fx0, fy0, cs, sn, shift), c10 = det_coord(fx1, fy0, cs, sn, shift);
         const float c01 = det_coord(fx0, fy1, cs, sn, shift), c11 = det_coord(fx1, fy1, cs, sn, shift);
         float lo = fminf(fminf(c00, c10), fminf(c01, c11));
         lo = fminf(fmaxf(lo, e0), e1);
-        S.w0[buf][tid] = (int) floorf(__fsub_rn(lo, 0.5f)) - 2;
+        int w0 = (int) floorf(__fsub_rn(lo, 0.5f)) - 2;
+        const int mis = (int) ((reinterpret_cast<uintptr_t>(sino + (size_t) a * P.n) >> 2) & 3);
+        w0 -= (w0 + mis) & 3;
+        S.ang[buf][tid] = make_float4(cs, sn, __int_as_float(w0), 0.0f);
     }
     __syncthreads();
-    /* windows: 256 threads, 4 angles x 64 detectors per round */
-    for (int idx = tid; idx < count * kWin; idx += kTX * kTY) {
-        const int slot = idx / kWin, e = idx % kWin;
+    constexpr int kGroups = kWin / 4;
+    for (int idx = tid; idx < count * kGroups; idx += kTX * kTY) {
+        const int slot = idx / kGroups, g = idx % kGroups;
         const int a = angle_of(P, first + slot);
-        const int d = S.w0[buf][slot] + e;
-        float *dst = &S.win[buf][slot][e];
-        if (d >= 0 && d < P.n)
-            cp_async4(dst, sino + (size_t) a * P.n + d);
-        else
-            *dst = 0.0f;
+        const int d = __float_as_int(S.ang[buf][slot].z) + 4 * g;
+        float *dst = &S.win[buf][slot][4 * g];
+        const float *src = sino + (size_t) a * P.n + d;
+        if (d >= 0 && d + 4 <= P.n) {
+            cp_async16(dst, src);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (d + e >= 0 && d + e < P.n)
+                    cp_async4(dst + e, src + e);
+                else
+                    dst[e] = 0.0f;
+            }
+        }
     }
 }
 
-template <bool CLAMP>
+/*
+ * All angles of one staged chunk for the thread's 8 pixels, two pixels per
+ * packed instruction. FAST: every clamped coordinate is >= 0.5, so the
+ * three-step floor applies.
+ */
+template <bool CLAMP, bool FAST>
 __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count, int first_vi, const BpTileArgs &P,
-                                             float fX, const float fY[kPY], float shift, float e0, float e1,
-                                             float sum[kPY], float v[kPY], int &sub, int &sub_end)
+                                             float fX, const float2 nfY[kPY / 2], float shift, float e0, float e1,
+                                             float2 sum[kPY / 2], float2 v[kPY / 2], int &sub, int &sub_end)
 {
+    const uint32_t win0 = (uint32_t) __cvta_generic_to_shared(&S.win[buf][0][0]);
+    const uint32_t bits = FAST ? (uint32_t) joseph::kHalfFloorBits : (uint32_t) joseph::kFloorMagicBits;
+    const float2 shift2 = joseph::splat(shift);
+    const float2 z2 = joseph::splat(P.neg_zero);
     for (int i = 0; i < count; ++i) {
         const int vi = first_vi + i;
         if (vi == sub_end) {
             /* end of a subset: v = v + relax * sum (one BP launch of the reference) */
 #pragma unroll
-            for (int p = 0; p < kPY; ++p) {
-                v[p] = __fadd_rn(v[p], __fmul_rn(P.relax, sum[p]));
-                sum[p] = 0.0f;
+            for (int q = 0; q < kPY / 2; ++q) {
+                v[q] = joseph::add2(v[q], joseph::mul2z(joseph::splat(P.relax), sum[q], joseph::splat(P.neg_zero)));
+                sum[q] = make_float2(0.0f, 0.0f);
             }
             ++sub;
             sub_end += (int) P.sub_n[sub];
         }
-        const float cs = S.cs[buf][i], sn = S.sn[buf][i];
-        const int w0 = S.w0[buf][i];
-        const float *win = S.win[buf][i];
-        const float fxc = __fmul_rn(fX, cs);
+        const float4 ang = S.ang[buf][i];
+        /* shared address of detector 0 of this angle's window, less the floor bits */
+        const uint32_t base = win0 + 4u * (uint32_t) (i * kWin) - 4u * ((uint32_t) __float_as_int(ang.z) + bits);
+        const float2 fxc = joseph::splat(__fmul_rn(fX, ang.x));
+        const float2 sn = joseph::splat(ang.y);
 #pragma unroll
-        for (int p = 0; p < kPY; ++p) {
-            float sc = __fadd_rn(__fsub_rn(fxc, __fmul_rn(fY[p], sn)), shift);
-            if (CLAMP)
-                sc = fminf(fmaxf(sc, e0), e1);
-            const float cm = __fsub_rn(sc, 0.5f);
-            const float y = __fadd_rd(cm, kFloorMagic);
-            const float fi = __fsub_rn(y, kFloorMagic);
-            const int j = __float_as_int(y) - kFloorMagicBits - w0;
-            const float t = __fsub_rn(cm, fi);
-            sum[p] = __fadd_rn(sum[p], joseph::lerp(t, win[j], win[j + 1]));
+        for (int q = 0; q < kPY / 2; ++q) {
+            /* fX * cos - fY * sin + shift, as fX*cos + (-fY)*sin + shift */
+            float2 sc = joseph::add2(joseph::add2(fxc, joseph::mul2z(nfY[q], sn, z2)), shift2);
+            if (CLAMP) {
+                sc.x = fminf(fmaxf(sc.x, e0), e1);
+                sc.y = fminf(fmaxf(sc.y, e0), e1);
+            }
+            float2 t;
+            const float2 y = FAST ? joseph::floor_half2(sc, t) : joseph::floor_any2(sc, t);
+            const uint32_t a0 = base + 4u * (uint32_t) __float_as_int(y.x);
+            const uint32_t a1 = base + 4u * (uint32_t) __float_as_int(y.y);
+            const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
+            const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
+            sum[q] = joseph::add2(sum[q], joseph::lerp2(t, t0, t1, z2));
         }
     }
 }
@@ -170,9 +212,9 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
 {
     __shared__ BpSmem S;
     const int n = P.n;
-    const int tiles_x = (n + kTile - 1) / kTile;
-    const int x0 = (int) (blockIdx.x % tiles_x) * kTile;
-    const int y0 = (int) (blockIdx.x / tiles_x) * kTile;
+    const int tiles_x = (n + kTileX - 1) / kTileX;
+    const int x0 = (int) (blockIdx.x % tiles_x) * kTileX;
+    const int y0 = (int) (blockIdx.x / tiles_x) * kTileY;
     const int slice = (int) blockIdx.y;
     const float *sino = P.sino + (size_t) slice * P.sino_stride;
 
@@ -183,26 +225,37 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
 
     const int x = x0 + (int) threadIdx.x;
     const float fX = __fsub_rn(__fadd_rn((float) x, 0.5f), k.os);
-    float fY[kPY], sum[kPY], v[kPY];
+    /* pixel pairs (p, p + 1) of the thread's column; -fY so that the
+     * coordinate is fX*cos + (-fY)*sin + shift */
+    float2 nfY[kPY / 2], sum[kPY / 2], v[kPY / 2];
 #pragma unroll
-    for (int p = 0; p < kPY; ++p) {
-        const int y = y0 + (int) threadIdx.y + kTY * p;
-        fY[p] = __fsub_rn(__fadd_rn((float) y, 0.5f), k.os);
-        sum[p] = 0.0f;
-        const size_t pix = (size_t) slice * P.vol_stride + (size_t) y * n + x;
-        v[p] = (P.base && x < n && y < n) ? P.base[pix] : 0.0f;
+    for (int q = 0; q < kPY / 2; ++q) {
+        float f[2], b[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int y = y0 + (int) threadIdx.y + kTY * (2 * q + h);
+            f[h] = -__fsub_rn(__fadd_rn((float) y, 0.5f), k.os);
+            const size_t pix = (size_t) slice * P.vol_stride + (size_t) y * n + x;
+            b[h] = (P.base && x < n && y < n) ? P.base[pix] : 0.0f;
+        }
+        nfY[q] = make_float2(f[0], f[1]);
+        v[q] = make_float2(b[0], b[1]);
+        sum[q] = make_float2(0.0f, 0.0f);
     }
 
     /* A tile whose every pixel lies within distance (n/2 - 2) of the centre
      * never reaches the clamp edges (on-axis geometry), so the clamp can be
-     * skipped without changing any result. */
+     * skipped without changing any result; its coordinates lie in
+     * [2, n - 2]. */
     bool clamp = true;
     if (k.diff == 0.0f) {
         const float r = 0.5f * (float) n - 2.0f;
-        const float ax = fmaxf(fabsf((float) x0 - k.os), fabsf((float) (x0 + kTile) - k.os));
-        const float ay = fmaxf(fabsf((float) y0 - k.os), fabsf((float) (y0 + kTile) - k.os));
+        const float ax = fmaxf(fabsf((float) x0 - k.os), fabsf((float) (x0 + kTileX) - k.os));
+        const float ay = fmaxf(fabsf((float) y0 - k.os), fabsf((float) (y0 + kTileY) - k.os));
         clamp = ax * ax + ay * ay > r * r;
     }
+    /* clamped coordinates are >= min(e0, e1) */
+    const bool fast = fminf(e0, e1) >= 0.5f;
 
     const int nchunks = (P.total_angles + kAC - 1) / kAC;
     int sub = 0;
@@ -222,16 +275,18 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
         }
         __syncthreads();
         const int count = min(kAC, P.total_angles - ch * kAC);
-        if (clamp)
-            sample_chunk<true>(S, buf, count, ch * kAC, P, fX, fY, shift, e0, e1, sum, v, sub, sub_end);
+        if (!clamp)
+            sample_chunk<false, true>(S, buf, count, ch * kAC, P, fX, nfY, shift, e0, e1, sum, v, sub, sub_end);
+        else if (fast)
+            sample_chunk<true, true>(S, buf, count, ch * kAC, P, fX, nfY, shift, e0, e1, sum, v, sub, sub_end);
         else
-            sample_chunk<false>(S, buf, count, ch * kAC, P, fX, fY, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, false>(S, buf, count, ch * kAC, P, fX, nfY, shift, e0, e1, sum, v, sub, sub_end);
         __syncthreads();
     }
     if (P.n_subsets > 0) {
 #pragma unroll
-        for (int p = 0; p < kPY; ++p)
-            v[p] = __fadd_rn(v[p], __fmul_rn(P.relax, sum[p]));
+        for (int q = 0; q < kPY / 2; ++q)
+            v[q] = joseph::add2(v[q], joseph::mul2z(joseph::splat(P.relax), sum[q], joseph::splat(P.neg_zero)));
     }
     if (x >= n)
         return;
@@ -240,7 +295,7 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
         const int y = y0 + (int) threadIdx.y + kTY * p;
         if (y >= n)
             continue;
-        float r = v[p];
+        float r = (p & 1) ? v[p >> 1].y : v[p >> 1].x;
         if (P.cw)
             r = __fmul_rn(r, P.cw[(size_t) slice * P.cw_stride + (size_t) y * n + x]);
         const size_t pix = (size_t) slice * P.vol_stride + (size_t) y * n + x;
@@ -288,12 +343,19 @@ extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *su
     A.cw_stride = cw_shared ? 0 : A.vol_stride;
     A.n_subsets = n_subsets;
     A.total_angles = total;
+    A.neg_zero = -0.0f;
+    A.contiguous = 1;
+    A.first_angle = n_subsets > 0 ? (int) subsets[0].offset : 0;
+    for (int i = 1; i < n_subsets; i++)
+        if (subsets[i].offset != subsets[i - 1].offset + subsets[i - 1].n)
+            A.contiguous = 0;
     for (int i = 0; i < kMaxSub; i++) {
         A.sub_offset[i] = i < n_subsets ? subsets[i].offset : 0;
         A.sub_n[i] = i < n_subsets ? subsets[i].n : 0;
     }
-    const int tiles_x = (g->n_dets + kTile - 1) / kTile;
-    const unsigned int n_tiles = (unsigned int) (tiles_x * tiles_x);
+    const int tiles_x = (g->n_dets + kTileX - 1) / kTileX;
+    const int tiles_y = (g->n_dets + kTileY - 1) / kTileY;
+    const unsigned int n_tiles = (unsigned int) (tiles_x * tiles_y);
     for (int done = 0; done < n_slices;) {
         const int chunk = n_slices - done > 65535 ? 65535 : n_slices - done;
         BpTileArgs B = A;

@@ -30,8 +30,8 @@
 namespace {
 
 constexpr int kPadL = 2;
-constexpr float kFloorMagic = 12582912.0f;      /* 1.5 * 2^23 */
-constexpr int kFloorMagicBits = 0x4B400000;
+/* bits of floor(c - 0.5) + 1.5 * 2^23, less the padded column of index 0 */
+constexpr int kColBits = joseph::kFloorMagicBits - kPadL;
 
 struct FpTileArgs {
     const float *volP;
@@ -50,6 +50,7 @@ struct FpTileArgs {
     long long volp_stride;
     long long sino_stride;
     long long w_stride;
+    float neg_zero;        /* -0.0f: the addend of unfusable packed products */
     int *err;
 };
 
@@ -70,21 +71,33 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
     const float *img = (dir == 0 ? P.volTP : P.volP) + (size_t) slice * P.volp_stride;
 
     const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
-    float c[A][J], inner[A][J], sum[A][J], stp[A];
+    /* rays of angles (2h, 2h + 1) travel as a pair through packed FP32 */
+    constexpr int H = A / 2;
+    float2 c[H][J], inner[H][J], sum[H][J], stp[H];
 #pragma unroll
-    for (int a = 0; a < A; ++a) {
-        stp[a] = 0.0f;
-        float det_step = 0.0f;
-        if (a < tile.y) {
-            const int angle = tile.x + a;
-            joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, stp[a]);
+    for (int h = 0; h < H; ++h) {
+        float st2[2], c2[2][J];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int a = 2 * h + e;
+            st2[e] = 0.0f;
+            float det_step = 0.0f;
+            if (a < tile.y) {
+                const int angle = tile.x + a;
+                joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, st2[e]);
+            }
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int s = (int) threadIdx.x + j * (int) blockDim.x;
+                c2[e][j] = (a < tile.y && s < n) ? joseph::ray_start(kc, s, n, det_step, st2[e]) : 0.0f;
+            }
         }
+        stp[h] = make_float2(st2[0], st2[1]);
 #pragma unroll
         for (int j = 0; j < J; ++j) {
-            const int s = (int) threadIdx.x + j * (int) blockDim.x;
-            c[a][j] = (a < tile.y && s < n) ? joseph::ray_start(kc, s, n, det_step, stp[a]) : 0.0f;
-            inner[a][j] = 0.0f;
-            sum[a][j] = 0.0f;
+            c[h][j] = make_float2(c2[0][j], c2[1][j]);
+            inner[h][j] = make_float2(0.0f, 0.0f);
+            sum[h][j] = make_float2(0.0f, 0.0f);
         }
     }
 
@@ -107,7 +120,12 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
         }
     }
 
-    const float hi = (float) n + 0.5f;
+    /* A tap pair starts at padded column floor(c - 0.5) + kPadL; pairs that
+     * start outside [0, n + 2] lie wholly in the zero border, so the start
+     * is clamped (as unsigned) to n + 2, whose taps are two pad zeros. */
+    const uint32_t col_lim = (uint32_t) n + 2u;
+    const float2 z2 = joseph::splat(P.neg_zero);
+    const uint32_t stage_s = (uint32_t) __cvta_generic_to_shared(stage0);
     bool ok = true;
     int waited = 0;
     for (int ch = 0; ch < nchunks; ++ch) {
@@ -119,30 +137,30 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
         const int r0 = ch * K;
         const int rows = min(K, n - r0);
         if (ok) {
-            const float *sbuf = stage0 + st * stage_floats + kPadL;
-            for (int r = 0; r < rows; ++r) {
-                const float *row = sbuf + (size_t) r * pitch;
+            uint32_t row_s = stage_s + 4u * (uint32_t) (st * (int) stage_floats);
+            for (int r = 0; r < rows; ++r, row_s += 4u * (uint32_t) pitch) {
 #pragma unroll
-                for (int a = 0; a < A; ++a) {
+                for (int h = 0; h < H; ++h) {
 #pragma unroll
                     for (int j = 0; j < J; ++j) {
-                        float cm = __fsub_rn(c[a][j], 0.5f);
-                        cm = fminf(fmaxf(cm, -1.5f), hi);
-                        const float y = __fadd_rd(cm, kFloorMagic);
-                        const float fi = __fsub_rn(y, kFloorMagic);
-                        const int i0 = __float_as_int(y) - kFloorMagicBits;
-                        const float t = __fsub_rn(cm, fi);
-                        inner[a][j] = __fadd_rn(inner[a][j], joseph::lerp(t, row[i0], row[i0 + 1]));
-                        c[a][j] = __fadd_rn(c[a][j], stp[a]);
+                        float2 t;
+                        const float2 y = joseph::floor_any2(c[h][j], t);
+                        const uint32_t p0 = min((uint32_t) (__float_as_int(y.x) - kColBits), col_lim);
+                        const uint32_t p1 = min((uint32_t) (__float_as_int(y.y) - kColBits), col_lim);
+                        const uint32_t a0 = row_s + 4u * p0, a1 = row_s + 4u * p1;
+                        const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
+                        const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
+                        inner[h][j] = joseph::add2(inner[h][j], joseph::lerp2(t, t0, t1, z2));
+                        c[h][j] = joseph::add2(c[h][j], stp[h]);
                     }
                 }
                 if (((r0 + r + 1) & 63) == 0) {
 #pragma unroll
-                    for (int a = 0; a < A; ++a)
+                    for (int h = 0; h < H; ++h)
 #pragma unroll
                         for (int j = 0; j < J; ++j) {
-                            sum[a][j] = __fadd_rn(sum[a][j], inner[a][j]);
-                            inner[a][j] = 0.0f;
+                            sum[h][j] = joseph::add2(sum[h][j], inner[h][j]);
+                            inner[h][j] = make_float2(0.0f, 0.0f);
                         }
                 }
             }
@@ -169,10 +187,10 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
 
     if ((n & 63) != 0) {
 #pragma unroll
-        for (int a = 0; a < A; ++a)
+        for (int h = 0; h < H; ++h)
 #pragma unroll
             for (int j = 0; j < J; ++j)
-                sum[a][j] = __fadd_rn(sum[a][j], inner[a][j]);
+                sum[h][j] = joseph::add2(sum[h][j], inner[h][j]);
     }
 #pragma unroll
     for (int a = 0; a < A; ++a) {
@@ -186,8 +204,9 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
                 continue;
             const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + s;
             float result = P.src[oidx];
+            const float ray = (a & 1) ? sum[a >> 1][j].y : sum[a >> 1][j].x;
             if (!joseph::detector_inactive(kc, s))
-                result = __fadd_rn(result, __fmul_rn(sum[a][j], P.scale));
+                result = __fadd_rn(result, __fmul_rn(ray, P.scale));
             if (P.w)
                 result = __fmul_rn(result, P.w[(size_t) slice * P.w_stride + (size_t) angle * n + s]);
             P.out[oidx] = result;
@@ -346,6 +365,7 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
     A.volp_stride = (long long) n * A.pitch;
     A.sino_stride = (long long) g->n_angles * n;
     A.w_stride = w_shared ? 0 : A.sino_stride;
+    A.neg_zero = -0.0f;
     A.err = d->d_err;
     switch (cfg.J * 16 + cfg.A) {
     case 1 * 16 + 8: return launch_tiles<1, 8>(d, A, n_tiles, n_slices, cfg);
