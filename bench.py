@@ -39,6 +39,13 @@ METRIC = "SIRT slice-iters/s @1024²×1200 ang; serve p50/p99 latency vs plain p
 N_DETS, N_ANGLES, PHANTOM, SLICES, I0, RELAX = 1448, 1200, 1024, 64, 1e5, 0.25
 E2E_ITERS = 10
 CPU_SAMPLE_ANGLES = 300
+# serve trace: the configured request mix, scaled to seconds of GPU time
+SERVE_JOBS = 16
+SERVE_RATE = 200.0
+SERVE_SIZES = ((256, 367), (512, 724), (1024, 1448), (2048, 2900))
+SERVE_ITER_SCALE = 100
+SERVE_BUDGET = 150 * 10**9
+SERVE_SEED = 5005
 
 
 def dist_env():
@@ -266,6 +273,9 @@ def run_ufoir(args, dist):
     e2e, per_job = None, {}
     if not args.quick:
         e2e, per_job = end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S)
+    serve = None
+    if not args.quick and not args.no_serve and dist.rank == 0:
+        serve = serve_section(ufoir, ctx)
 
     # roofline of the dominant kernel (live CUDA-event durations above)
     peak, peak_kind = measured_peaks()
@@ -301,6 +311,8 @@ def run_ufoir(args, dist):
                       "parallelism": "replicas: slices sharded across ranks, no collective"},
            "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "roofline": roofline,
            "kernel_ms": kernel_ms, "sample_rate": sample_rate, **per_job}
+    if serve is not None:
+        out["serve"] = serve
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and not args.quick:
         out["cpu_baseline"] = cpu_baseline(noisy[0])
     d_sino.close()
@@ -343,6 +355,84 @@ def end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S):
     return e2e, per_job
 
 
+def serve_trace(ufoir, ctx):
+    """A scaled copy of the serve workload: the configured job distributions
+    (phantom side P in {256, 512, 1024, 2048} -> grid n in {367, 724, 1448,
+    2900}; angles U{90..1800}; method in {SART, SIRT, ASD-POCS}; iterations
+    U{10..200}) with Poisson arrivals at 200 jobs/s, cut to SERVE_JOBS jobs and
+    iterations / SERVE_ITER_SCALE so that one pass takes seconds."""
+    from ufoir import synth
+    rng = np.random.default_rng(SERVE_SEED)
+    methods = (ufoir.METHOD_SART, ufoir.METHOD_SIRT, ufoir.METHOD_ASDPOCS)
+    jobs, t, samples = [], 0.0, 0.0
+    cache = {}
+    for i in range(SERVE_JOBS):
+        t += float(rng.exponential(1.0 / SERVE_RATE))
+        P, n = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
+        na = int(rng.integers(90, 1801))
+        method = methods[int(rng.integers(3))]
+        iters = max(1, int(round(int(rng.integers(10, 201)) / SERVE_ITER_SCALE)))
+        step = float(np.float32(np.pi / na))
+        if n not in cache:
+            cache[n] = synth.ellipse_phantom(n, P, 10, seed=SERVE_SEED + n)
+        proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=1)
+        sino = np.zeros((na, n), np.float32)
+        proj.forward(cache[n], sino)
+        proj.close()
+        if method == ufoir.METHOD_ASDPOCS:
+            desc = ufoir.job_desc(method, n, na, step, asdpocs=dict(num_iterations=iters))
+            per_iter = 10
+        else:
+            desc = ufoir.job_desc(method, n, na, step, num_iterations=iters)
+            per_iter = 1
+        samples += iters * per_iter * 2.0 * n * n * na
+        jobs.append((t, desc, sino, method, n, na, iters))
+    return jobs, samples
+
+
+def run_serve(ufoir, ctx, jobs, policy):
+    """Submits the trace at its arrival times from one host thread and waits for all jobs."""
+    with ufoir.Server(ctx, hbm_budget=SERVE_BUDGET, policy=policy) as srv:
+        t0 = time.perf_counter()
+        ids = []
+        for (t, desc, sino, *_rest) in jobs:
+            delay = t - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(srv.submit(desc, sino)[0])
+        rc = srv.drain(600000)
+        st = srv.stats()
+        st["wall_s"] = time.perf_counter() - t0
+        st["drain_status"] = rc
+    return st
+
+
+def serve_section(ufoir, ctx):
+    """The same scaled trace through the continuous-batching loop and through
+    the one-job-at-a-time loop (the plain per-job path)."""
+    jobs, samples = serve_trace(ufoir, ctx)
+    span = jobs[-1][0]
+    out = {"trace": {"jobs": len(jobs), "arrival": f"Poisson, {SERVE_RATE:g} jobs/s (seed {SERVE_SEED})",
+                     "offered_window_s": span, "offered_jobs_per_s": len(jobs) / span if span > 0 else None,
+                     "offered_samples": samples,
+                     "sizes": "phantom P in {256,512,1024,2048} -> grid n in {367,724,1448,2900}",
+                     "angles": "U{90..1800}", "methods": "SART / SIRT / ASD-POCS (uniform)",
+                     "iterations": f"U{{10..200}} / {SERVE_ITER_SCALE} (rounded, >= 1); ASD-POCS: outer "
+                                   "iterations, inner SART num-iterations 10",
+                     "hbm_budget_bytes": SERVE_BUDGET,
+                     "mix": {m: sum(1 for j in jobs if j[3] == k) for m, k in
+                             (("sart", ufoir.METHOD_SART), ("sirt", ufoir.METHOD_SIRT),
+                              ("asdpocs", ufoir.METHOD_ASDPOCS))}}}
+    keys = ("completed", "failed", "p50_latency_ms", "p99_latency_ms", "mean_latency_ms", "max_latency_ms",
+            "p50_queue_ms", "p99_queue_ms", "throughput_jobs_per_s", "busy_seconds", "peak_hbm_bytes",
+            "peak_active_jobs", "wall_s")
+    for name, pol in (("one_at_a_time", ufoir.SERVE_ONE_AT_A_TIME), ("continuous", ufoir.SERVE_CONTINUOUS)):
+        st = run_serve(ufoir, ctx, jobs, pol)
+        out[name] = {k: st[k] for k in keys if k in st}
+        out[name]["samples_per_s"] = samples / st["busy_seconds"] if st.get("busy_seconds") else None
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,7 +442,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slices", type=int, default=SLICES, help="slices per GPU (64 = the headline workload)")
     ap.add_argument("--quick", action="store_true",
-                    help="only the resident timed steps (skip e2e, per-job comparison, CPU baseline)")
+                    help="only the resident timed steps (skip e2e, per-job comparison, serve trace, CPU baseline)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serve trace")
     args = ap.parse_args()
     dist = Dist()
     try:

@@ -45,7 +45,8 @@ def test_sirt_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, sli
 
 
 @pytest.mark.parametrize("n,na,axis,iters,slices", [(16, 12, -1.0, 2, 1), (33, 40, 15.3, 2, 2),
-                                                     (48, 36, -1.0, 1, 1)])
+                                                     (48, 36, -1.0, 1, 1), (100, 60, -1.0, 1, 2),
+                                                     (130, 50, 64.7, 2, 1)])
 def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
     rng = np.random.default_rng(3 * n + na)
     step = np.float32(np.pi / na)

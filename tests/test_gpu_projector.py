@@ -53,8 +53,10 @@ def test_golden_fixtures(ufoir_lib, gpu_ctx, path):
     assert rel_l2(x, d["sart"]) <= 1e-4 and np.array_equal(x, d["sart"])
 
 
+# the last two put the axis within half a pixel of an image edge, where the
+# backprojector's clamp edges cross (e0 > e1)
 CASES = [(7, 5, -1.0), (16, 12, -1.0), (33, 40, 15.3), (33, 40, 17.9), (64, 90, -1.0),
-         (100, 180, -1.0), (61, 36, 31.25), (128, 7, -1.0)]
+         (100, 180, -1.0), (61, 36, 31.25), (128, 7, -1.0), (24, 30, 0.25), (24, 30, 23.8)]
 
 
 @pytest.mark.parametrize("n,na,axis", CASES)

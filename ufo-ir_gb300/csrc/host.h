@@ -68,7 +68,9 @@ typedef struct {
 } ufoir__sirt_iter;
 int ufoir__sirt_body(void *arg);
 
-/* One SART sweep (every angle in order) over n_slices slices. */
+/* One SART sweep (every angle in order) over n_slices slices. xT holds the
+ * volume transposed during the horizontal direction run; table holds the
+ * block-start coordinates of the per-angle forward projection. */
 typedef struct {
     ufoir_projector *p;
     udev_geom g;
@@ -77,8 +79,12 @@ typedef struct {
     const float *R;
     float lambda;
     int n_slices;
+    float *xT, *table;
 } ufoir__sart_iter;
 int ufoir__sart_body(void *arg);
+/* The sweep's scratch (xT, table; the geometry must be prepared). */
+int ufoir__sart_scratch_alloc(ufoir_projector *p, float **xT, float **table, int n_slices);
+size_t ufoir__sart_scratch_bytes(size_t n, size_t na, size_t n_slices);
 
 /* ASD-POCS split into setup, one outer iteration and release, so that the
  * plain call and the serve loop run the same code. */
@@ -91,6 +97,7 @@ typedef struct {
     const float *b;
     float *out;
     float *x, *x_prev, *x_res, *b_res, *grad, *R;
+    float *xT, *table;                  /* SART sweep scratch */
     ufoir_fp_scratch fs;
     float *dp, *dd, *dg, *dtgv, *l1;    /* per-slice host scalars */
     float beta, sart_relax;

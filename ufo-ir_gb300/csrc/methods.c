@@ -376,25 +376,52 @@ int ufoir__sart_body(void *arg)
 {
     ufoir__sart_iter *s = (ufoir__sart_iter *) arg;
     udev *d = s->p->ctx->dev;
+    const int n = s->g.n_dets, S = s->n_slices;
     int rc = UFOIR_OK;
     /* sart-task.c:209-217: per angle, r_theta = (b_theta - A_theta x) * R_theta;
-     * x = x + lambda A_theta^T r_theta. */
+     * x = x + lambda A_theta^T r_theta. The volume is held transposed while
+     * the angles are horizontal, so that every ray walks rows. */
+    int transposed = 0;
     for (unsigned int a = 0; a < s->p->n_angles && rc == UFOIR_OK; a++) {
-        ufoir_subset sub;
-        sub.offset = a;
-        sub.n = 1;
-        sub.direction = s->p->h_dir[a];
-        rc = udev_fp(d, &s->g, (int) a, 1, sub.direction, s->x, NULL, s->b, s->R, 1, s->resid, -1.0f,
-                     s->n_slices);
+        const int dir = s->p->h_dir[a];
+        const int want = dir == UFOIR_HORIZONTAL;
+        if (want != transposed) {
+            rc = udev_transpose(d, transposed ? s->xT : s->x, transposed ? s->x : s->xT, n, S);
+            transposed = want;
+        }
+        float *vol = transposed ? s->xT : s->x;
         if (!rc)
-            rc = udev_bp(d, &s->g, &sub, 1, s->resid, s->x, NULL, 0, NULL, s->x, s->lambda, s->n_slices);
+            rc = udev_fp_angle(d, &s->g, (int) a, dir, s->table, vol, s->b, s->R, 1, s->resid, -1.0f, S);
+        if (!rc)
+            rc = udev_bp_angle(d, &s->g, (int) a, s->resid, vol, transposed, s->lambda, S);
     }
+    if (!rc && transposed)
+        rc = udev_transpose(d, s->xT, s->x, n, S);
+    return rc;
+}
+
+size_t ufoir__sart_scratch_bytes(size_t n, size_t na, size_t n_slices)
+{
+    return sizeof(float) * (n * n * n_slices + udev_fp_block_starts_floats((int) n, (int) na));
+}
+
+int ufoir__sart_scratch_alloc(ufoir_projector *p, float **xT, float **table, int n_slices)
+{
+    ufoir_ctx *ctx = p->ctx;
+    const size_t n = p->n_dets;
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    int rc = ufoir__alloc(ctx, xT, n * n * (size_t) n_slices);
+    if (!rc)
+        rc = ufoir__alloc(ctx, table, udev_fp_block_starts_floats((int) n, (int) p->n_angles));
+    if (!rc)
+        rc = udev_fp_block_starts(ctx->dev, &g, *table);
     return rc;
 }
 
 /* One SART call on resident buffers: x = SART(b), R precomputed. */
 static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, const float *b, float *x,
-                    float *resid, const float *R, int n_slices)
+                    float *resid, const float *R, float *xT, float *table, int n_slices)
 {
     ufoir_ctx *ctx = proj->ctx;
     const size_t n = proj->n_dets, nv = n * n;
@@ -412,6 +439,8 @@ static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, con
     it.R = R;
     it.lambda = lambda;
     it.n_slices = n_slices;
+    it.xT = xT;
+    it.table = table;
     /* one angle sweep per graph: a sweep is already 2 * n_angles kernels */
     int rc2 = UFOIR_OK;
     void *exec = NULL;
@@ -447,19 +476,22 @@ int ufoir_sart_process(ufoir_projector *proj, const ufoir_sart_params *prm, cons
         return rc;
     const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
     ufoir_buf bb = {0}, bx = {0};
-    float *R = NULL, *resid = NULL;
+    float *R = NULL, *resid = NULL, *xT = NULL, *table = NULL;
     UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
     UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices > nv ? ns * n_slices : nv));
+    UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &xT, &table, (int) n_slices));
     proj->prm.correction_scale = 1.0f;
     UFOIR_TRY(ufoir__ray_weights(proj, R, resid));
-    UFOIR_TRY(sart_run(proj, prm->num_iterations, prm->relaxation_factor, bb.dev, bx.dev, resid, R,
+    UFOIR_TRY(sart_run(proj, prm->num_iterations, prm->relaxation_factor, bb.dev, bx.dev, resid, R, xT, table,
                        (int) n_slices));
     UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
 done:
     ufoir__free(ctx, R);
     ufoir__free(ctx, resid);
+    ufoir__free(ctx, xT);
+    ufoir__free(ctx, table);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bx);
     udev_sync(ctx->dev);
@@ -498,15 +530,17 @@ void ufoir__asd_release(ufoir__asd_state *s)
     ufoir__free(ctx, s->b_res);
     ufoir__free(ctx, s->grad);
     ufoir__free(ctx, s->R);
+    ufoir__free(ctx, s->xT);
+    ufoir__free(ctx, s->table);
     ufoir__fp_scratch_free(s->p, &s->fs);
-    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = NULL;
+    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = s->xT = s->table = NULL;
 }
 
 size_t ufoir__asd_bytes(size_t n, size_t na, size_t S)
 {
     const size_t nv = n * n, ns = n * na, pitch = (size_t) udev_fp_pitch((int) n);
     const size_t bres = ns * S > nv ? ns * S : nv;
-    return sizeof(float) * (4 * nv * S + bres + ns + 2 * n * pitch * S);
+    return sizeof(float) * (4 * nv * S + bres + ns + 2 * n * pitch * S) + ufoir__sart_scratch_bytes(n, na, S);
 }
 
 /* Buffers, weights and the first state of asdpocs-task.c:411-455. The
@@ -534,6 +568,7 @@ int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asd
     UFOIR_TRY(ufoir__alloc(ctx, &s->b_res, ns * S > nv ? ns * S : nv));
     UFOIR_TRY(ufoir__alloc(ctx, &s->grad, nv * S));
     UFOIR_TRY(ufoir__alloc(ctx, &s->R, ns));
+    UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &s->xT, &s->table, S));
     UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &s->fs, (size_t) S));
     s->dp = (float *) calloc((size_t) S * 5, sizeof(float));
     if (!s->dp) {
@@ -575,7 +610,8 @@ int ufoir__asd_outer(ufoir__asd_state *s)
      * property's range is [0, 1] and GObject rejects values outside it. */
     if (s->beta >= 0.0f && s->beta <= 1.0f)
         s->sart_relax = s->beta;
-    if ((rc = sart_run(proj, prm->df_minimizer.num_iterations, s->sart_relax, s->b, s->x, s->b_res, s->R, S)))
+    if ((rc = sart_run(proj, prm->df_minimizer.num_iterations, s->sart_relax, s->b, s->x, s->b_res, s->R, s->xT,
+                       s->table, S)))
         return rc;
     if (prm->positive_constraint && (rc = udev_unary(d, UDEV_POSC, s->x, 0, 0, s->x, nv * S)))
         return rc;

@@ -66,6 +66,21 @@ int udev_fp(udev *d, const udev_geom *g, int a0, int na, int dir_override,
 /* Transpose n x n slices. */
 int udev_transpose(udev *d, const float *in, float *out, int n, int n_slices);
 
+/* ---- Per-angle projections of a SART sweep (udev_sart.cu) ---- */
+/* Floats of the block-start table: the coordinate of every ray of every
+ * angle at the start of each 64-sample block, [n_angles][ceil(n/64)][n]. */
+size_t udev_fp_block_starts_floats(int n, int n_angles);
+int udev_fp_block_starts(udev *d, const udev_geom *g, float *table);
+/* Forward projection of one angle, rays walking the rows of img (the volume
+ * for vertical rays, dir 1; its transpose for horizontal rays, dir 0):
+ *   out = (src + scale * S) [* w]  for the angle's row of the sinogram. */
+int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, const float *table, const float *img,
+                  const float *src, const float *w, int w_shared, float *out, float scale, int n_slices);
+/* vol = vol + relax * A_angle^T sino (one-angle subset), in place; with
+ * transposed != 0, vol holds the transpose of the volume. */
+int udev_bp_angle(udev *d, const udev_geom *g, int angle, const float *sino, float *vol, int transposed,
+                  float relax, int n_slices);
+
 /* ---- Tiled forward projector (all angles, shared-memory row streaming) ---- */
 /* Row pitch (floats, multiple of 4) of the padded images: 2 zero columns,
  * n values, at least 2 zero columns. */

@@ -71,33 +71,35 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
     const float *img = (dir == 0 ? P.volTP : P.volP) + (size_t) slice * P.volp_stride;
 
     const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
-    /* rays of angles (2h, 2h + 1) travel as a pair through packed FP32 */
-    constexpr int H = A / 2;
-    float2 c[H][J], inner[H][J], sum[H][J], stp[H];
+    /* Lanes: each warp holds 16 detector slots x 2 adjacent angles (the
+     * half-warp g takes the tile's angles g, g + 2, g + 4, ...). Rays of
+     * adjacent angles through adjacent detectors meet a row within ~25
+     * words, so a warp's shared loads stay free of bank conflicts, which 32
+     * adjacent detectors of one angle (spread 1/|cos| apart) are not.
+     * A thread owns A/2 angles x 2J detectors d0 + i * half; detectors
+     * (2m, 2m + 1) of one angle travel as a pair through packed FP32. */
+    constexpr int A2 = A / 2;
+    const int lane = (int) (threadIdx.x & 31);
+    const int g = lane >> 4;
+    const int half = (int) (blockDim.x >> 1);
+    const int d0 = (int) (threadIdx.x >> 5) * 16 + (lane & 15);
+    float2 c[A2][J], inner[A2][J], sum[A2][J], stp[A2];
 #pragma unroll
-    for (int h = 0; h < H; ++h) {
-        float st2[2], c2[2][J];
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int a = 2 * h + e;
-            st2[e] = 0.0f;
-            float det_step = 0.0f;
-            if (a < tile.y) {
-                const int angle = tile.x + a;
-                joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, st2[e]);
-            }
-#pragma unroll
-            for (int j = 0; j < J; ++j) {
-                const int s = (int) threadIdx.x + j * (int) blockDim.x;
-                c2[e][j] = (a < tile.y && s < n) ? joseph::ray_start(kc, s, n, det_step, st2[e]) : 0.0f;
-            }
+    for (int k = 0; k < A2; ++k) {
+        const int a = g + 2 * k;
+        float st = 0.0f, det_step = 0.0f;
+        if (a < tile.y) {
+            const int angle = tile.x + a;
+            joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, st);
         }
-        stp[h] = make_float2(st2[0], st2[1]);
+        stp[k] = joseph::splat(st);
 #pragma unroll
-        for (int j = 0; j < J; ++j) {
-            c[h][j] = make_float2(c2[0][j], c2[1][j]);
-            inner[h][j] = make_float2(0.0f, 0.0f);
-            sum[h][j] = make_float2(0.0f, 0.0f);
+        for (int m = 0; m < J; ++m) {
+            const int s0 = d0 + 2 * m * half, s1 = s0 + half;
+            c[k][m] = make_float2((a < tile.y && s0 < n) ? joseph::ray_start(kc, s0, n, det_step, st) : 0.0f,
+                                  (a < tile.y && s1 < n) ? joseph::ray_start(kc, s1, n, det_step, st) : 0.0f);
+            inner[k][m] = make_float2(0.0f, 0.0f);
+            sum[k][m] = make_float2(0.0f, 0.0f);
         }
     }
 
@@ -140,27 +142,27 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
             uint32_t row_s = stage_s + 4u * (uint32_t) (st * (int) stage_floats);
             for (int r = 0; r < rows; ++r, row_s += 4u * (uint32_t) pitch) {
 #pragma unroll
-                for (int h = 0; h < H; ++h) {
+                for (int k = 0; k < A2; ++k) {
 #pragma unroll
-                    for (int j = 0; j < J; ++j) {
+                    for (int m = 0; m < J; ++m) {
                         float2 t;
-                        const float2 y = joseph::floor_any2(c[h][j], t);
+                        const float2 y = joseph::floor_any2(c[k][m], t);
                         const uint32_t p0 = min((uint32_t) (__float_as_int(y.x) - kColBits), col_lim);
                         const uint32_t p1 = min((uint32_t) (__float_as_int(y.y) - kColBits), col_lim);
                         const uint32_t a0 = row_s + 4u * p0, a1 = row_s + 4u * p1;
                         const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
                         const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
-                        inner[h][j] = joseph::add2(inner[h][j], joseph::lerp2(t, t0, t1, z2));
-                        c[h][j] = joseph::add2(c[h][j], stp[h]);
+                        inner[k][m] = joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
+                        c[k][m] = joseph::add2(c[k][m], stp[k]);
                     }
                 }
                 if (((r0 + r + 1) & 63) == 0) {
 #pragma unroll
-                    for (int h = 0; h < H; ++h)
+                    for (int k = 0; k < A2; ++k)
 #pragma unroll
-                        for (int j = 0; j < J; ++j) {
-                            sum[h][j] = joseph::add2(sum[h][j], inner[h][j]);
-                            inner[h][j] = make_float2(0.0f, 0.0f);
+                        for (int m = 0; m < J; ++m) {
+                            sum[k][m] = joseph::add2(sum[k][m], inner[k][m]);
+                            inner[k][m] = make_float2(0.0f, 0.0f);
                         }
                 }
             }
@@ -187,24 +189,25 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
 
     if ((n & 63) != 0) {
 #pragma unroll
-        for (int h = 0; h < H; ++h)
+        for (int k = 0; k < A2; ++k)
 #pragma unroll
-            for (int j = 0; j < J; ++j)
-                sum[h][j] = joseph::add2(sum[h][j], inner[h][j]);
+            for (int m = 0; m < J; ++m)
+                sum[k][m] = joseph::add2(sum[k][m], inner[k][m]);
     }
 #pragma unroll
-    for (int a = 0; a < A; ++a) {
+    for (int k = 0; k < A2; ++k) {
+        const int a = g + 2 * k;
         if (a >= tile.y)
             continue;
         const int angle = tile.x + a;
 #pragma unroll
-        for (int j = 0; j < J; ++j) {
-            const int s = (int) threadIdx.x + j * (int) blockDim.x;
+        for (int i = 0; i < 2 * J; ++i) {
+            const int s = d0 + i * half;
             if (s >= n)
                 continue;
             const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + s;
             float result = P.src[oidx];
-            const float ray = (a & 1) ? sum[a >> 1][j].y : sum[a >> 1][j].x;
+            const float ray = (i & 1) ? sum[k][i >> 1].y : sum[k][i >> 1].x;
             if (!joseph::detector_inactive(kc, s))
                 result = __fadd_rn(result, __fmul_rn(ray, P.scale));
             if (P.w)
@@ -253,7 +256,9 @@ TileCfg tile_cfg(int n, int smem_optin)
     TileCfg c;
     c.J = n <= 768 ? 1 : (n <= 1536 ? 2 : (n <= 3072 ? 4 : 8));
     c.A = c.J <= 2 ? 8 : (c.J == 4 ? 4 : 2);
-    c.threads = (int) (((n + c.J - 1) / c.J + 31) / 32 * 32);
+    /* 16 detector slots per warp and angle group, 2J detectors per slot */
+    const int slots = (n + 2 * c.J - 1) / (2 * c.J);
+    c.threads = (slots + 15) / 16 * 32;
     const int pitch = udev_fp_pitch(n);
     c.K = 32;
     while (c.K > 4 && 128 + 2 * (size_t) c.K * pitch * 4 > (size_t) smem_optin)

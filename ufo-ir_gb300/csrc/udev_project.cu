@@ -272,8 +272,15 @@ extern "C" int udev_bp(udev *d, const udev_geom *g, const ufoir_subset *subsets,
         }
         total += subsets[i].n;
     }
+    /* The tiled kernel clamps with min/max, which equals the reference's
+     * if / else-if clamp (…joseph.cl:206-210) only while e0 <= e1; an axis
+     * within half a pixel of the image edge gives e0 > e1 and goes to the
+     * gather kernel, which follows the reference's form. */
+    const float n_f = (float) g->n_dets;
+    const float half = n_f - g->axis * 2.0f < 0.0f ? n_f - g->axis : g->axis;
+    const bool edges_ordered = g->axis - half + 0.5f <= g->axis + half - 0.5f;
     /* many angles: the tiled kernel (shared-memory sinogram windows) */
-    if (total >= 16 && n_subsets <= 16)
+    if (total >= 16 && n_subsets <= 16 && edges_ordered)
         return udev_bp_tiles(d, g, subsets, n_subsets, sino, base, cw, cw_shared, add, dst, relax, n_slices);
     UDEV_BIND(d);
     BpArgs A;

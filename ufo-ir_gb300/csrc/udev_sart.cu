@@ -1,0 +1,257 @@
+/*
+ * udev_sart.cu - the per-angle projections of SART (and of ASD-POCS, whose
+ * data-fidelity step is SART): one angle's forward projection, then one
+ * angle's backprojection, n_angles times per sweep (sart-task.c:209-217).
+ *
+ * One angle is only n rays of n samples, so a ray-per-thread kernel leaves
+ * the GPU idle. Here a ray is cut into its 64-sample blocks (the blocks the
+ * reference sums separately, projector-parallel-joseph.cl:81-93) and every
+ * (ray, block) pair is a thread. The coordinate at each block start is the
+ * float recurrence c += step replayed from the ray start; it depends only on
+ * the geometry, so it is tabulated once per job (block_starts_kernel) and a
+ * block's thread starts from the table with the exact value the sequential
+ * walk reaches. The block sums of a ray are then added in order in shared
+ * memory, exactly as the reference adds its inner sums.
+ *
+ * Rays walk rows of a row-major image: vertical rays the volume, horizontal
+ * rays its transpose. SART keeps the volume in the layout of the current
+ * direction run (the angles of [0, pi) form three runs) and transposes it
+ * at the two run boundaries; the per-angle backprojection updates either
+ * layout in place.
+ */
+#include <cuda_runtime.h>
+
+#include "joseph.cuh"
+#include "udev_internal.cuh"
+
+namespace {
+
+constexpr int kBlock = 64;          /* samples per block (the reference's BLOCK_SIZE) */
+constexpr int kRaysPerCta = 8;      /* lanes: 8 rays x 4 blocks per warp */
+constexpr int kMaxBlocks = 128;     /* n <= 8192 */
+
+__global__ void __launch_bounds__(256) block_starts_kernel(const float *__restrict__ sinv,
+                                                           const float *__restrict__ cosv,
+                                                           const unsigned char *__restrict__ dirs, int n,
+                                                           int n_blocks, float axis, float *__restrict__ table)
+{
+    const int s = (int) (blockIdx.x * blockDim.x + threadIdx.x);
+    const int a = (int) blockIdx.y;
+    if (s >= n)
+        return;
+    const joseph::AxisConsts k = joseph::axis_consts(n, axis);
+    float det_step, step;
+    joseph::ray_steps((int) dirs[a], sinv[a], cosv[a], det_step, step);
+    float c = joseph::ray_start(k, s, n, det_step, step);
+    float *t = table + (size_t) a * n_blocks * n + s;
+    for (int b = 0; b < n_blocks; ++b) {
+        t[(size_t) b * n] = c;
+#pragma unroll 8
+        for (int r = 0; r < kBlock; ++r)
+            c = __fadd_rn(c, step);
+    }
+}
+
+struct FpAngleArgs {
+    const float *img;       /* rows walked by this angle's rays */
+    const float *table;     /* [n_angles][n_blocks][n] block-start coordinates */
+    const float *src;
+    const float *w;
+    float *out;
+    const float *sinv;
+    const float *cosv;
+    int n;
+    int n_blocks;
+    int angle;
+    int dir;
+    float axis;
+    float scale;
+    long long img_stride;
+    long long sino_stride;
+    long long w_stride;
+};
+
+/* out = (src + scale * S) [* w] for the rays of one angle. Grid
+ * (ceil(n / 8), slices); block 32 * ceil(n_blocks / 4) threads. */
+__global__ void __launch_bounds__(1024) fp_angle_kernel(FpAngleArgs P)
+{
+    __shared__ float bsum[kMaxBlocks][kRaysPerCta];
+    const int lane = (int) (threadIdx.x & 31);
+    const int ray = lane & (kRaysPerCta - 1);
+    const int b = (int) (threadIdx.x >> 5) * 4 + (lane >> 3);
+    const int s = (int) blockIdx.x * kRaysPerCta + ray;
+    const int slice = (int) blockIdx.y;
+    const int n = P.n;
+
+    if (s < n && b < P.n_blocks) {
+        float det_step, step;
+        joseph::ray_steps(P.dir, P.sinv[P.angle], P.cosv[P.angle], det_step, step);
+        const float *img = P.img + (size_t) slice * P.img_stride;
+        float c = P.table[((size_t) P.angle * P.n_blocks + b) * n + s];
+        const int row0 = b * kBlock;
+        const int rows = min(kBlock, n - row0);
+        float inner = 0.0f;
+#pragma unroll 8
+        for (int r = 0; r < rows; ++r) {
+            const float *row = img + (size_t) (row0 + r) * n;
+            int i0;
+            float t;
+            joseph::lerp_coord(c, i0, t);
+            const float t0 = (unsigned) i0 < (unsigned) n ? __ldg(row + i0) : 0.0f;
+            const float t1 = (unsigned) (i0 + 1) < (unsigned) n ? __ldg(row + i0 + 1) : 0.0f;
+            inner = __fadd_rn(inner, joseph::lerp(t, t0, t1));
+            c = __fadd_rn(c, step);
+        }
+        bsum[b][ray] = inner;
+    }
+    __syncthreads();
+    if (threadIdx.x < kRaysPerCta && s < n) {
+        const size_t oidx = (size_t) slice * P.sino_stride + (size_t) P.angle * n + s;
+        float result = P.src[oidx];
+        const joseph::AxisConsts k = joseph::axis_consts(n, P.axis);
+        if (!joseph::detector_inactive(k, s)) {
+            float detected = 0.0f;
+            for (int j = 0; j < P.n_blocks; ++j)
+                detected = __fadd_rn(detected, bsum[j][ray]);
+            result = __fadd_rn(result, __fmul_rn(detected, P.scale));
+        }
+        if (P.w)
+            result = __fmul_rn(result, P.w[(size_t) slice * P.w_stride + (size_t) P.angle * n + s]);
+        P.out[oidx] = result;
+    }
+}
+
+struct BpAngleArgs {
+    const float *sino;
+    float *vol;
+    const float *sinv;
+    const float *cosv;
+    int n;
+    int angle;
+    int transposed;     /* vol holds the transpose: element (i, j) is pixel x = i, y = j */
+    float axis;
+    float relax;
+    long long vol_stride;
+    long long sino_stride;
+};
+
+/* vol = vol + relax * (0 + sample) for one angle (…joseph.cl:158-218 with a
+ * one-angle subset). Grid (ceil(n / 32), ceil(n / 8), slices), block 32 x 8. */
+__global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
+{
+    const int i = (int) (blockIdx.x * blockDim.x + threadIdx.x);   /* storage column */
+    const int j = (int) (blockIdx.y * blockDim.y + threadIdx.y);   /* storage row */
+    const int slice = (int) blockIdx.z;
+    const int n = P.n;
+    if (i >= n || j >= n)
+        return;
+    const int x = P.transposed ? j : i;
+    const int y = P.transposed ? i : j;
+    const joseph::AxisConsts k = joseph::axis_consts(n, P.axis);
+    float e0, e1;
+    joseph::bp_edges(k, n, P.axis, e0, e1);
+    const float shift = __fsub_rn(k.os, k.ros);
+    const float fX = __fsub_rn(__fadd_rn((float) x, 0.5f), k.os);
+    const float fY = __fsub_rn(__fadd_rn((float) y, 0.5f), k.os);
+    const float sn = __ldg(P.sinv + P.angle), cs = __ldg(P.cosv + P.angle);
+    float sc = __fadd_rn(__fsub_rn(__fmul_rn(fX, cs), __fmul_rn(fY, sn)), shift);
+    if (sc > e1)
+        sc = e1;
+    else if (sc < e0)
+        sc = e0;
+    int i0;
+    float t;
+    joseph::lerp_coord(sc, i0, t);
+    const float *r = P.sino + (size_t) slice * P.sino_stride + (size_t) P.angle * n;
+    const float sum = __fadd_rn(0.0f, joseph::lerp(t, joseph::texel(r, i0, n), joseph::texel(r, i0 + 1, n)));
+    const size_t p = (size_t) slice * P.vol_stride + (size_t) j * n + i;
+    P.vol[p] = __fadd_rn(P.vol[p], __fmul_rn(P.relax, sum));
+}
+
+}  // namespace
+
+extern "C" size_t udev_fp_block_starts_floats(int n, int n_angles)
+{
+    const int nb = (n + kBlock - 1) / kBlock;
+    return (size_t) n_angles * nb * n;
+}
+
+extern "C" int udev_fp_block_starts(udev *d, const udev_geom *g, float *table)
+{
+    const int n = g->n_dets;
+    if (n <= 0 || g->n_angles <= 0)
+        return UFOIR_OK;
+    if (n > kMaxBlocks * kBlock || g->n_angles > 65535) {
+        udev_set_error(d, "sart: n = %d, n_angles = %d beyond the per-angle kernels' limits (%d, 65535)", n,
+                       g->n_angles, kMaxBlocks * kBlock);
+        return UFOIR_ERR_UNSUPPORTED;
+    }
+    UDEV_BIND(d);
+    const int nb = (n + kBlock - 1) / kBlock;
+    dim3 grid(udev_div_up(n, 256), (unsigned int) g->n_angles);
+    block_starts_kernel<<<grid, 256, 0, d->stream>>>(g->d_sin, g->d_cos, g->d_dir, n, nb, g->axis, table);
+    return udev_after_launch(d, "block_starts_kernel");
+}
+
+extern "C" int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, const float *table, const float *img,
+                             const float *src, const float *w, int w_shared, float *out, float scale, int n_slices)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    const int n = g->n_dets;
+    if (angle < 0 || angle >= g->n_angles || n > kMaxBlocks * kBlock || n_slices > 65535) {
+        udev_set_error(d, "fp_angle: angle %d of %d, n = %d, %d slices out of range", angle, g->n_angles, n,
+                       n_slices);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    FpAngleArgs A;
+    A.img = img;
+    A.table = table;
+    A.src = src;
+    A.w = w;
+    A.out = out;
+    A.sinv = g->d_sin;
+    A.cosv = g->d_cos;
+    A.n = n;
+    A.n_blocks = (n + kBlock - 1) / kBlock;
+    A.angle = angle;
+    A.dir = dir;
+    A.axis = g->axis;
+    A.scale = scale;
+    A.img_stride = (long long) n * n;
+    A.sino_stride = (long long) g->n_angles * n;
+    A.w_stride = w_shared ? 0 : A.sino_stride;
+    const int threads = 32 * ((A.n_blocks + 3) / 4);
+    dim3 grid(udev_div_up(n, kRaysPerCta), (unsigned int) n_slices);
+    fp_angle_kernel<<<grid, threads, 0, d->stream>>>(A);
+    return udev_after_launch(d, "fp_angle_kernel");
+}
+
+extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, const float *sino, float *vol, int transposed,
+                             float relax, int n_slices)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    const int n = g->n_dets;
+    if (angle < 0 || angle >= g->n_angles || n_slices > 65535) {
+        udev_set_error(d, "bp_angle: angle %d of %d, %d slices out of range", angle, g->n_angles, n_slices);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    BpAngleArgs A;
+    A.sino = sino;
+    A.vol = vol;
+    A.sinv = g->d_sin;
+    A.cosv = g->d_cos;
+    A.n = n;
+    A.angle = angle;
+    A.transposed = transposed;
+    A.axis = g->axis;
+    A.relax = relax;
+    A.vol_stride = (long long) n * n;
+    A.sino_stride = (long long) g->n_angles * n;
+    dim3 grid(udev_div_up(n, 32), udev_div_up(n, 8), (unsigned int) n_slices);
+    bp_angle_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    return udev_after_launch(d, "bp_angle_kernel");
+}
