@@ -393,7 +393,8 @@ int ufoir__sart_body(void *arg)
         if (!rc)
             rc = udev_fp_angle(d, &s->g, (int) a, dir, s->table, vol, s->b, s->R, 1, s->resid, -1.0f, S);
         if (!rc)
-            rc = udev_bp_angle(d, &s->g, (int) a, s->resid, vol, transposed, s->lambda, S);
+            rc = udev_bp_angle(d, &s->g, (int) a, s->p->h_sin[a], s->p->h_cos[a], s->resid, vol, transposed,
+                               s->lambda, S);
     }
     if (!rc && transposed)
         rc = udev_transpose(d, s->xT, s->x, n, S);

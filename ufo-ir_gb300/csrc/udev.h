@@ -77,9 +77,10 @@ int udev_fp_block_starts(udev *d, const udev_geom *g, float *table);
 int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, const float *table, const float *img,
                   const float *src, const float *w, int w_shared, float *out, float scale, int n_slices);
 /* vol = vol + relax * A_angle^T sino (one-angle subset), in place; with
- * transposed != 0, vol holds the transpose of the volume. */
-int udev_bp_angle(udev *d, const udev_geom *g, int angle, const float *sino, float *vol, int transposed,
-                  float relax, int n_slices);
+ * transposed != 0, vol holds the transpose of the volume. sn, cs: the
+ * angle's entries of the float LUT. */
+int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino, float *vol,
+                  int transposed, float relax, int n_slices);
 
 /* ---- Tiled forward projector (all angles, shared-memory row streaming) ---- */
 /* Row pitch (floats, multiple of 4) of the padded images: 2 zero columns,

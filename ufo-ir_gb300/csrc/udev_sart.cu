@@ -29,6 +29,8 @@ namespace {
 constexpr int kBlock = 64;          /* samples per block (the reference's BLOCK_SIZE) */
 constexpr int kRaysPerCta = 8;      /* lanes: 8 rays x 4 blocks per warp */
 constexpr int kMaxBlocks = 128;     /* n <= 8192 */
+constexpr int kGroup = 16;          /* samples whose loads are issued together */
+constexpr int kMaxThreads = 512;
 
 __global__ void __launch_bounds__(256) block_starts_kernel(const float *__restrict__ sinv,
                                                            const float *__restrict__ cosv,
@@ -72,35 +74,53 @@ struct FpAngleArgs {
 };
 
 /* out = (src + scale * S) [* w] for the rays of one angle. Grid
- * (ceil(n / 8), slices); block 32 * ceil(n_blocks / 4) threads. */
-__global__ void __launch_bounds__(1024) fp_angle_kernel(FpAngleArgs P)
+ * (ceil(n / 8), slices); block 32 * min(16, ceil(n_blocks / 4)) threads,
+ * thread (ray, b0) taking blocks b0, b0 + blockDim / 8, ... */
+__global__ void __launch_bounds__(kMaxThreads) fp_angle_kernel(FpAngleArgs P)
 {
     __shared__ float bsum[kMaxBlocks][kRaysPerCta];
     const int lane = (int) (threadIdx.x & 31);
     const int ray = lane & (kRaysPerCta - 1);
-    const int b = (int) (threadIdx.x >> 5) * 4 + (lane >> 3);
     const int s = (int) blockIdx.x * kRaysPerCta + ray;
     const int slice = (int) blockIdx.y;
     const int n = P.n;
 
-    if (s < n && b < P.n_blocks) {
+    for (int b = (int) (threadIdx.x >> 5) * 4 + (lane >> 3); s < n && b < P.n_blocks;
+         b += (int) blockDim.x / kRaysPerCta) {
         float det_step, step;
         joseph::ray_steps(P.dir, P.sinv[P.angle], P.cosv[P.angle], det_step, step);
         const float *img = P.img + (size_t) slice * P.img_stride;
         float c = P.table[((size_t) P.angle * P.n_blocks + b) * n + s];
         const int row0 = b * kBlock;
         const int rows = min(kBlock, n - row0);
+        const float *row = img + (size_t) row0 * n;
         float inner = 0.0f;
-#pragma unroll 8
-        for (int r = 0; r < rows; ++r) {
-            const float *row = img + (size_t) (row0 + r) * n;
-            int i0;
-            float t;
-            joseph::lerp_coord(c, i0, t);
-            const float t0 = (unsigned) i0 < (unsigned) n ? __ldg(row + i0) : 0.0f;
-            const float t1 = (unsigned) (i0 + 1) < (unsigned) n ? __ldg(row + i0 + 1) : 0.0f;
-            inner = __fadd_rn(inner, joseph::lerp(t, t0, t1));
-            c = __fadd_rn(c, step);
+        /* Groups of kGroup samples: the coordinates first (the float
+         * recurrence), then all loads (unconditional, indices clamped into
+         * the row; the zero border is applied afterwards), then the in-order
+         * sum, so that 2 * kGroup loads are in flight per thread. */
+        for (int g0 = 0; g0 < rows; g0 += kGroup) {
+            int i0[kGroup];
+            float t[kGroup], va[kGroup], vb[kGroup];
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) {
+                joseph::lerp_coord(c, i0[k], t[k]);
+                c = __fadd_rn(c, step);
+            }
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) {
+                const float *rr = row + (size_t) min(g0 + k, rows - 1) * n;
+                va[k] = __ldg(rr + min(max(i0[k], 0), n - 1));
+                vb[k] = __ldg(rr + min(max(i0[k] + 1, 0), n - 1));
+            }
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) {
+                if (g0 + k < rows) {
+                    const float t0 = (unsigned) i0[k] < (unsigned) n ? va[k] : 0.0f;
+                    const float t1 = (unsigned) (i0[k] + 1) < (unsigned) n ? vb[k] : 0.0f;
+                    inner = __fadd_rn(inner, joseph::lerp(t[k], t0, t1));
+                }
+            }
         }
         bsum[b][ray] = inner;
     }
@@ -124,48 +144,49 @@ __global__ void __launch_bounds__(1024) fp_angle_kernel(FpAngleArgs P)
 struct BpAngleArgs {
     const float *sino;
     float *vol;
-    const float *sinv;
-    const float *cosv;
     int n;
     int angle;
     int transposed;     /* vol holds the transpose: element (i, j) is pixel x = i, y = j */
-    float axis;
+    float os, shift, e0, e1;   /* origin shift, os - ros, clamp edges (…joseph.cl:174-187) */
+    float sn, cs;
     float relax;
     long long vol_stride;
     long long sino_stride;
 };
 
 /* vol = vol + relax * (0 + sample) for one angle (…joseph.cl:158-218 with a
- * one-angle subset). Grid (ceil(n / 32), ceil(n / 8), slices), block 32 x 8. */
+ * one-angle subset). Grid (ceil(n / 64), ceil(n / 8), slices), block 32 x 8;
+ * a thread updates storage columns i and i + 32 of one storage row. */
 __global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
 {
-    const int i = (int) (blockIdx.x * blockDim.x + threadIdx.x);   /* storage column */
     const int j = (int) (blockIdx.y * blockDim.y + threadIdx.y);   /* storage row */
     const int slice = (int) blockIdx.z;
     const int n = P.n;
-    if (i >= n || j >= n)
+    if (j >= n)
         return;
-    const int x = P.transposed ? j : i;
-    const int y = P.transposed ? i : j;
-    const joseph::AxisConsts k = joseph::axis_consts(n, P.axis);
-    float e0, e1;
-    joseph::bp_edges(k, n, P.axis, e0, e1);
-    const float shift = __fsub_rn(k.os, k.ros);
-    const float fX = __fsub_rn(__fadd_rn((float) x, 0.5f), k.os);
-    const float fY = __fsub_rn(__fadd_rn((float) y, 0.5f), k.os);
-    const float sn = __ldg(P.sinv + P.angle), cs = __ldg(P.cosv + P.angle);
-    float sc = __fadd_rn(__fsub_rn(__fmul_rn(fX, cs), __fmul_rn(fY, sn)), shift);
-    if (sc > e1)
-        sc = e1;
-    else if (sc < e0)
-        sc = e0;
-    int i0;
-    float t;
-    joseph::lerp_coord(sc, i0, t);
     const float *r = P.sino + (size_t) slice * P.sino_stride + (size_t) P.angle * n;
-    const float sum = __fadd_rn(0.0f, joseph::lerp(t, joseph::texel(r, i0, n), joseph::texel(r, i0 + 1, n)));
-    const size_t p = (size_t) slice * P.vol_stride + (size_t) j * n + i;
-    P.vol[p] = __fadd_rn(P.vol[p], __fmul_rn(P.relax, sum));
+    const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int i = (int) (blockIdx.x * 64 + threadIdx.x) + 32 * h;   /* storage column */
+        if (i >= n)
+            break;
+        const float fI = __fsub_rn(__fadd_rn((float) i, 0.5f), P.os);
+        const float fX = P.transposed ? fJ : fI;
+        const float fY = P.transposed ? fI : fJ;
+        float sc = __fadd_rn(__fsub_rn(__fmul_rn(fX, P.cs), __fmul_rn(fY, P.sn)), P.shift);
+        if (sc > P.e1)
+            sc = P.e1;
+        else if (sc < P.e0)
+            sc = P.e0;
+        int i0;
+        float t;
+        joseph::lerp_coord(sc, i0, t);
+        const float sum =
+            __fadd_rn(0.0f, joseph::lerp(t, joseph::texel(r, i0, n), joseph::texel(r, i0 + 1, n)));
+        const size_t p = (size_t) slice * P.vol_stride + (size_t) j * n + i;
+        P.vol[p] = __fadd_rn(P.vol[p], __fmul_rn(P.relax, sum));
+    }
 }
 
 }  // namespace
@@ -222,14 +243,15 @@ extern "C" int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, co
     A.img_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
     A.w_stride = w_shared ? 0 : A.sino_stride;
-    const int threads = 32 * ((A.n_blocks + 3) / 4);
+    const int warps = (A.n_blocks + 3) / 4;
+    const int threads = 32 * (warps < kMaxThreads / 32 ? warps : kMaxThreads / 32);
     dim3 grid(udev_div_up(n, kRaysPerCta), (unsigned int) n_slices);
     fp_angle_kernel<<<grid, threads, 0, d->stream>>>(A);
     return udev_after_launch(d, "fp_angle_kernel");
 }
 
-extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, const float *sino, float *vol, int transposed,
-                             float relax, int n_slices)
+extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino,
+                             float *vol, int transposed, float relax, int n_slices)
 {
     if (n_slices <= 0)
         return UFOIR_OK;
@@ -239,19 +261,29 @@ extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, const float
         return UFOIR_ERR_INVALID;
     }
     UDEV_BIND(d);
+    /* the per-launch constants of …joseph.cl:174-187 (float arithmetic,
+     * the multiplications and divisions by 2 exact) */
+    const float w = (float) n, axis = g->axis;
+    const float required_width = axis * 2.0f;
+    const float diff = w - required_width;
+    const float ros = diff / 2.0f, os = w / 2.0f;
+    const float half = diff < 0.0f ? w - axis : axis;
     BpAngleArgs A;
     A.sino = sino;
     A.vol = vol;
-    A.sinv = g->d_sin;
-    A.cosv = g->d_cos;
     A.n = n;
     A.angle = angle;
     A.transposed = transposed;
-    A.axis = g->axis;
+    A.os = os;
+    A.shift = os - ros;
+    A.e0 = axis - half + 0.5f;
+    A.e1 = axis + half - 0.5f;
+    A.sn = sn;
+    A.cs = cs;
     A.relax = relax;
     A.vol_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
-    dim3 grid(udev_div_up(n, 32), udev_div_up(n, 8), (unsigned int) n_slices);
+    dim3 grid(udev_div_up(n, 64), udev_div_up(n, 8), (unsigned int) n_slices);
     bp_angle_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(A);
     return udev_after_launch(d, "bp_angle_kernel");
 }
