@@ -312,10 +312,12 @@ typedef struct {
 
 typedef struct {
     uint64_t hbm_budget_bytes;        /* 0 = the context's budget */
-    unsigned int max_active_jobs;     /* 0 = 32 */
+    unsigned int max_active_jobs;     /* jobs admitted (resident) at once; 0 = 32 */
     int policy;                       /* UFOIR_SERVE_* */
     unsigned int quantum;             /* SIRT iterations / SART sweeps per scheduling turn; 0 = 1 */
     unsigned int fail_allocation_every; /* testing: make every k-th job allocation fail (0 = off) */
+    unsigned int max_running;         /* CONTINUOUS: jobs with work in flight at once, the ones
+                                         with the least remaining work first; 0 = 4 */
 } ufoir_serve_config;
 
 typedef struct {

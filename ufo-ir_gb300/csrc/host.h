@@ -80,6 +80,7 @@ typedef struct {
     float lambda;
     int n_slices;
     float *xT, *table;
+    const float *relax_dev;     /* if not NULL, lambda is read from here */
 } ufoir__sart_iter;
 int ufoir__sart_body(void *arg);
 /* The sweep's scratch (xT, table; the geometry must be prepared). */
@@ -99,8 +100,13 @@ typedef struct {
     float *x, *x_prev, *x_res, *b_res, *grad, *R;
     float *xT, *table;                  /* SART sweep scratch */
     ufoir_fp_scratch fs;
-    float *dp, *dd, *dg, *dtgv, *l1;    /* per-slice host scalars */
-    float beta, sart_relax;
+    float *scal;                        /* device scalar block (dsc points into it) */
+    double *partials;                   /* FP64 norm partials of this state */
+    udev_asd_scalars dsc;
+    ufoir__sart_iter sweep;
+    void *sart_exec, *post_exec;        /* graphs: one SART sweep; the rest of an outer iteration */
+    uint64_t sart_kernels, post_kernels;
+    float beta, sart_relax;             /* host copies of the float sequence, for the properties */
     unsigned int it;
 } ufoir__asd_state;
 int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *b,

@@ -394,7 +394,7 @@ int ufoir__sart_body(void *arg)
             rc = udev_fp_angle(d, &s->g, (int) a, dir, s->table, vol, s->b, s->R, 1, s->resid, -1.0f, S);
         if (!rc)
             rc = udev_bp_angle(d, &s->g, (int) a, s->p->h_sin[a], s->p->h_cos[a], s->resid, vol, transposed,
-                               s->lambda, S);
+                               s->lambda, s->relax_dev, S);
     }
     if (!rc && transposed)
         rc = udev_transpose(d, s->xT, s->x, n, S);
@@ -442,6 +442,7 @@ static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, con
     it.n_slices = n_slices;
     it.xT = xT;
     it.table = table;
+    it.relax_dev = NULL;
     /* one angle sweep per graph: a sweep is already 2 * n_angles kernels */
     int rc2 = UFOIR_OK;
     void *exec = NULL;
@@ -523,8 +524,9 @@ static int asdpocs_check(ufoir_ctx *ctx, const ufoir_asdpocs_params *prm)
 void ufoir__asd_release(ufoir__asd_state *s)
 {
     ufoir_ctx *ctx = s->p->ctx;
-    free(s->dp);
-    s->dp = NULL;
+    udev_graph_destroy(s->sart_exec);
+    udev_graph_destroy(s->post_exec);
+    s->sart_exec = s->post_exec = NULL;
     ufoir__free(ctx, s->x);
     ufoir__free(ctx, s->x_prev);
     ufoir__free(ctx, s->x_res);
@@ -533,19 +535,83 @@ void ufoir__asd_release(ufoir__asd_state *s)
     ufoir__free(ctx, s->R);
     ufoir__free(ctx, s->xT);
     ufoir__free(ctx, s->table);
+    ufoir__free(ctx, s->scal);
+    ufoir__free(ctx, s->partials);
     ufoir__fp_scratch_free(s->p, &s->fs);
-    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = s->xT = s->table = NULL;
+    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = s->xT = s->table = s->scal = NULL;
+    s->partials = NULL;
+}
+
+/* Floats of the device scalar block: beta, relax, it (as int bits), then
+ * dp, dd, dg, dtgv, l1 per slice. */
+static size_t asd_scalar_floats(size_t S)
+{
+    return 3 + 5 * S;
 }
 
 size_t ufoir__asd_bytes(size_t n, size_t na, size_t S)
 {
     const size_t nv = n * n, ns = n * na, pitch = (size_t) udev_fp_pitch((int) n);
     const size_t bres = ns * S > nv ? ns * S : nv;
-    return sizeof(float) * (4 * nv * S + bres + ns + 2 * n * pitch * S) + ufoir__sart_scratch_bytes(n, na, S);
+    return sizeof(float) * (4 * nv * S + bres + ns + 2 * n * pitch * S + asd_scalar_floats(S)) +
+           sizeof(double) * udev_l1_partials((int) S) + ufoir__sart_scratch_bytes(n, na, S);
 }
 
-/* Buffers, weights and the first state of asdpocs-task.c:411-455. The
- * geometry must be prepared; b and out are device memory (S slices). */
+/* The part of an outer iteration after the SART sweeps (asdpocs-task.c:461-506),
+ * for capture: every scalar stays on the device. */
+static int asd_post_body(void *arg)
+{
+    ufoir__asd_state *s = (ufoir__asd_state *) arg;
+    ufoir_projector *proj = s->p;
+    udev *d = proj->ctx->dev;
+    const size_t n = s->n, na = s->na, nv = s->nv;
+    const int S = s->S;
+    const ufoir_asdpocs_params *prm = &s->prm;
+    const udev_asd_scalars *c = &s->dsc;
+    int rc;
+    if (prm->positive_constraint && (rc = udev_unary(d, UDEV_POSC, s->x, 0, 0, s->x, nv * S)))
+        return rc;
+    if ((rc = udev_memcpy_async(d, s->out, s->x, nv * S * sizeof(float))))
+        return rc;
+    /* b_res = b - A x (:470-475) */
+    if ((rc = ufoir__fp_full(proj, &s->fs, s->x, s->b, NULL, 0, s->b_res, -1.0f, S)) ||
+        (rc = udev_l1_norm_to(d, s->b_res, n, na, S, prm->norm_mode, s->partials, c->dd)) ||
+        (rc = udev_binary(d, UDEV_SUB, s->x, s->x_prev, 0, s->x_res, nv * S)) ||
+        (rc = udev_l1_norm_to(d, s->x_res, n, n, S, prm->norm_mode, s->partials, c->dp)) ||
+        (rc = udev_asd_init(d, c, prm->alpha, S)) ||
+        (rc = udev_memcpy_async(d, s->x_prev, s->x, nv * S * sizeof(float))))
+        return rc;
+    /* ufo_math_tvstd_method_process_real (:550-580): 20 sub-steps */
+    for (int step = 0; step < 20; step++) {
+        if ((rc = udev_l1_grad(d, s->x, s->grad, (int) n, (int) n, S)) ||
+            (rc = udev_l1_norm_to(d, s->grad, n, n, S, prm->norm_mode, s->partials, c->l1)) ||
+            (rc = udev_asd_tv_step(d, s->x, s->grad, c, nv, S)))
+            return rc;
+    }
+    if ((rc = udev_binary(d, UDEV_SUB, s->x, s->x_prev, 0, s->x_res, nv * S)) ||
+        (rc = udev_l1_norm_to(d, s->x_res, n, n, S, prm->norm_mode, s->partials, c->dg)))
+        return rc;
+    return udev_asd_end(d, c, prm->beta_red, prm->r_max, prm->alpha_red, S);
+}
+
+static int capture(udev *d, int (*body)(void *), void *arg, void **exec, uint64_t *kernels)
+{
+    int rc = udev_capture_begin(d);
+    if (rc)
+        return rc;
+    rc = body(arg);
+    const int rc2 = udev_capture_end(d, exec, kernels);
+    if (rc || rc2) {
+        udev_graph_destroy(*exec);
+        *exec = NULL;
+        return rc ? rc : rc2;
+    }
+    return UFOIR_OK;
+}
+
+/* Buffers, weights, device scalars and the two graphs of an outer iteration
+ * (asdpocs-task.c:411-455). The geometry must be prepared; b and out are
+ * device memory (S slices). */
 int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *b,
                      float *out, int S)
 {
@@ -562,93 +628,97 @@ int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asd
     s->out = out;
     ufoir__projector_geom(proj, &s->g);
     const size_t nv = s->nv, ns = s->ns;
+    float *h = NULL;
     int rc;
+    if (S > 1024)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "ASD-POCS: %d slices in one call (at most 1024)", S);
     UFOIR_TRY(ufoir__alloc(ctx, &s->x, nv * S));
     UFOIR_TRY(ufoir__alloc(ctx, &s->x_prev, nv * S));
     UFOIR_TRY(ufoir__alloc(ctx, &s->x_res, nv * S));
     UFOIR_TRY(ufoir__alloc(ctx, &s->b_res, ns * S > nv ? ns * S : nv));
     UFOIR_TRY(ufoir__alloc(ctx, &s->grad, nv * S));
     UFOIR_TRY(ufoir__alloc(ctx, &s->R, ns));
+    UFOIR_TRY(ufoir__alloc(ctx, &s->scal, asd_scalar_floats((size_t) S)));
+    UFOIR_TRY(udev_malloc(ctx->dev, (void **) &s->partials, sizeof(double) * (udev_l1_partials(S) + 1)));
     UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &s->xT, &s->table, S));
     UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &s->fs, (size_t) S));
-    s->dp = (float *) calloc((size_t) S * 5, sizeof(float));
-    if (!s->dp) {
+    s->dsc.beta = s->scal;
+    s->dsc.relax = s->scal + 1;
+    s->dsc.it = (int *) (s->scal + 2);
+    s->dsc.dp = s->scal + 3;
+    s->dsc.dd = s->dsc.dp + S;
+    s->dsc.dg = s->dsc.dd + S;
+    s->dsc.dtgv = s->dsc.dg + S;
+    s->dsc.l1 = s->dsc.dtgv + S;
+    /* initial values (:418-455): beta, the minimizer's relaxation, it = 0,
+     * and the norms and TV step at 1 */
+    h = (float *) malloc(sizeof(float) * asd_scalar_floats((size_t) S));
+    if (!h) {
         rc = ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
         goto done;
     }
-    s->dd = s->dp + S;
-    s->dg = s->dd + S;
-    s->dtgv = s->dg + S;
-    s->l1 = s->dtgv + S;
-    for (int i = 0; i < S; i++)
-        s->dp[i] = s->dd[i] = s->dg[i] = s->dtgv[i] = 1.0f;
+    h[0] = prm->beta;
+    h[1] = prm->df_minimizer.relaxation_factor;
+    memset(&h[2], 0, sizeof(float));
+    for (size_t i = 3; i < asd_scalar_floats((size_t) S); i++)
+        h[i] = 1.0f;
+    UFOIR_TRY(udev_memcpy_async(ctx->dev, s->scal, h, sizeof(float) * asd_scalar_floats((size_t) S)));
     UFOIR_TRY(udev_fill(ctx->dev, s->x, nv * S, 0.0f));
     UFOIR_TRY(udev_fill(ctx->dev, s->x_prev, nv * S, 0.0f));
     /* SART's ray weights depend on the geometry only; the reference
      * recomputes the same values on every df_minimizer call. */
     proj->prm.correction_scale = 1.0f;
     UFOIR_TRY(ufoir__ray_weights(proj, s->R, s->b_res));
+    UFOIR_TRY(udev_sync(ctx->dev));     /* h is read by the copy above */
+    free(h);
+    h = NULL;
+    /* one SART sweep, relaxation read from the device scalar */
+    s->sweep.p = proj;
+    s->sweep.g = s->g;
+    s->sweep.b = b;
+    s->sweep.x = s->x;
+    s->sweep.resid = s->b_res;
+    s->sweep.R = s->R;
+    s->sweep.lambda = 0.0f;
+    s->sweep.relax_dev = s->dsc.relax;
+    s->sweep.n_slices = S;
+    s->sweep.xT = s->xT;
+    s->sweep.table = s->table;
+    UFOIR_TRY(capture(ctx->dev, ufoir__sart_body, &s->sweep, &s->sart_exec, &s->sart_kernels));
+    UFOIR_TRY(capture(ctx->dev, asd_post_body, s, &s->post_exec, &s->post_kernels));
     s->beta = prm->beta;
     s->sart_relax = prm->df_minimizer.relaxation_factor;
     s->it = 0;
     return UFOIR_OK;
 done:
+    free(h);
     ufoir__asd_release(s);
     return rc;
 }
 
-/* One outer iteration of asdpocs-task.c:457-506 (synchronous: the norms
- * come back to the host for the reference's float scalar logic). */
+/* One outer iteration of asdpocs-task.c:457-506, enqueued without any host
+ * synchronisation: the relaxation update, SART from x = 0 (sart-task.c:207),
+ * the SART sweeps, then the post-SART graph. */
 int ufoir__asd_outer(ufoir__asd_state *s)
 {
     ufoir_projector *proj = s->p;
     udev *d = proj->ctx->dev;
-    const size_t n = s->n, na = s->na, nv = s->nv;
-    const int S = s->S;
-    const ufoir_asdpocs_params *prm = &s->prm;
     int rc;
     /* g_object_set(df_minimizer, "relaxation_factor", beta) (:459); the
-     * property's range is [0, 1] and GObject rejects values outside it. */
+     * property's range is [0, 1] and GObject rejects values outside it. The
+     * host follows the same float sequence for the projector's properties. */
     if (s->beta >= 0.0f && s->beta <= 1.0f)
         s->sart_relax = s->beta;
-    if ((rc = sart_run(proj, prm->df_minimizer.num_iterations, s->sart_relax, s->b, s->x, s->b_res, s->R, s->xT,
-                       s->table, S)))
+    if ((rc = udev_asd_begin(d, &s->dsc)) || (rc = udev_fill(d, s->x, s->nv * (size_t) s->S, 0.0f)))
         return rc;
-    if (prm->positive_constraint && (rc = udev_unary(d, UDEV_POSC, s->x, 0, 0, s->x, nv * S)))
-        return rc;
-    if ((rc = udev_memcpy_async(d, s->out, s->x, nv * S * sizeof(float))))
-        return rc;
-    /* b_res = b - A x (:470-475) */
-    proj->prm.correction_scale = -1.0f;
-    if ((rc = ufoir__fp_full(proj, &s->fs, s->x, s->b, NULL, 0, s->b_res, -1.0f, S)) ||
-        (rc = udev_l1_norm(d, s->b_res, n, na, S, prm->norm_mode, s->dd)) ||
-        (rc = udev_binary(d, UDEV_SUB, s->x, s->x_prev, 0, s->x_res, nv * S)) ||
-        (rc = udev_l1_norm(d, s->x_res, n, n, S, prm->norm_mode, s->dp)))
-        return rc;
-    if (s->it == 0)
-        for (int i = 0; i < S; i++)
-            s->dtgv[i] = prm->alpha * s->dp[i];
-    if ((rc = udev_memcpy_async(d, s->x_prev, s->x, nv * S * sizeof(float))))
-        return rc;
-    /* ufo_math_tvstd_method_process_real (:550-580): 20 sub-steps */
-    for (int step = 0; step < 20; step++) {
-        if ((rc = udev_l1_grad(d, s->x, s->grad, (int) n, (int) n, S)) ||
-            (rc = udev_l1_norm(d, s->grad, n, n, S, prm->norm_mode, s->l1)))
+    for (unsigned int i = 0; i < s->prm.df_minimizer.num_iterations; i++)
+        if ((rc = udev_graph_launch(d, s->sart_exec, s->sart_kernels)))
             return rc;
-        for (int i = 0; i < S; i++) {
-            const float factor = s->dtgv[i] / s->l1[i];
-            if ((rc = udev_binary(d, UDEV_SUB_SCALED, s->x + (size_t) i * nv, s->grad + (size_t) i * nv, factor,
-                                  s->x + (size_t) i * nv, nv)))
-                return rc;
-        }
-    }
-    if ((rc = udev_binary(d, UDEV_SUB, s->x, s->x_prev, 0, s->x_res, nv * S)) ||
-        (rc = udev_l1_norm(d, s->x_res, n, n, S, prm->norm_mode, s->dg)))
+    if ((rc = udev_graph_launch(d, s->post_exec, s->post_kernels)))
         return rc;
-    s->beta *= prm->beta_red;
-    for (int i = 0; i < S; i++)
-        if (s->dg[i] > prm->r_max * s->dp[i] && s->dd[i] > 0.001f)
-            s->dtgv[i] *= prm->alpha_red;
+    proj->prm.relaxation = s->sart_relax;
+    proj->prm.correction_scale = -1.0f;
+    s->beta *= s->prm.beta_red;
     s->it++;
     return UFOIR_OK;
 }

@@ -22,6 +22,7 @@
 #include "host.h"
 
 #define DEFAULT_MAX_ACTIVE 32
+#define DEFAULT_MAX_RUNNING 4
 
 enum { PH_QUEUED = 0, PH_RUN = 1, PH_FINAL = 2, PH_END = 3 };
 
@@ -47,6 +48,7 @@ typedef struct job {
     void *graph;
     uint64_t graph_kernels;
     unsigned int done_iters, total_iters;
+    double work_per_iter;       /* interpolated samples of one quantum's iteration */
     struct job *next;
 } job;
 
@@ -88,6 +90,7 @@ void ufoir_serve_config_init(ufoir_serve_config *c)
     c->max_active_jobs = DEFAULT_MAX_ACTIVE;
     c->policy = UFOIR_SERVE_CONTINUOUS;
     c->quantum = 1;
+    c->max_running = DEFAULT_MAX_RUNNING;
 }
 
 void ufoir_job_desc_init(ufoir_job_desc *j)
@@ -114,6 +117,17 @@ static size_t job_bytes(const ufoir_job_desc *d)
     default:
         return sizeof(float) * (ns + nv + fs) + ufoir__asd_bytes(n, na, 1);
     }
+}
+
+/* Interpolated samples of one scheduling quantum's iteration: FP + BP over
+ * every angle (2 n^2 n_a); an ASD-POCS outer iteration is its SART sweeps
+ * plus one FP. Used to order jobs by remaining work. */
+static double job_work_per_iter(const ufoir_job_desc *d)
+{
+    const double n = d->n_dets, na = d->n_angles, pass = n * n * na;
+    if (d->method == UFOIR_METHOD_ASDPOCS)
+        return pass * (2.0 * d->asdpocs.df_minimizer.num_iterations + 1.0);
+    return 2.0 * pass;
 }
 
 static int check_desc(ufoir_ctx *ctx, const ufoir_job_desc *d)
@@ -363,6 +377,8 @@ static void *worker_main(void *arg)
     ufoir_server *s = (ufoir_server *) arg;
     const unsigned int max_active =
         s->cfg.policy == UFOIR_SERVE_ONE_AT_A_TIME ? 1 : (s->cfg.max_active_jobs ? s->cfg.max_active_jobs : DEFAULT_MAX_ACTIVE);
+    const unsigned int max_running =
+        s->cfg.policy == UFOIR_SERVE_ONE_AT_A_TIME ? 1 : (s->cfg.max_running ? s->cfg.max_running : DEFAULT_MAX_RUNNING);
     for (;;) {
         /* admission, in arrival order */
         job *admit[64];
@@ -414,38 +430,71 @@ static void *worker_main(void *arg)
             }
         }
         int progressed = n_admit > 0;
+        /* 1. completions; jobs whose iterations are done are finalized */
+        unsigned int running = 0;
+        job *idle[1024];
+        unsigned int n_idle = 0;
         for (unsigned int i = 0; i < n_list; i++) {
             job *j = list[i];
             if (j->phase == PH_END)
                 continue;
             if (j->busy) {
                 const int q = udev_event_done(s->ctx->dev, j->event);
-                if (q == 0)
+                if (q == 0) {
+                    running++;
                     continue;
+                }
                 j->busy = 0;
+                progressed = 1;
                 if (q < 0) {
                     j->phase = PH_END;
                     job_finish(s, j, q);
                     continue;
                 }
             }
-            int rc = UFOIR_OK;
-            if (j->phase == PH_RUN && j->done_iters < j->total_iters) {
-                rc = job_quantum(s, j);
-            } else if (j->phase == PH_RUN) {
-                rc = job_finalize(s, j);
-                j->phase = PH_FINAL;
-            } else if (j->phase == PH_FINAL) {
+            if (j->phase == PH_FINAL) {
                 j->phase = PH_END;
                 job_finish(s, j, UFOIR_OK);
                 progressed = 1;
-                continue;
+            } else if (j->phase == PH_RUN && j->done_iters >= j->total_iters) {
+                const int rc = job_finalize(s, j);
+                j->phase = PH_FINAL;
+                if (rc != UFOIR_OK) {
+                    j->phase = PH_END;
+                    job_finish(s, j, rc);
+                } else {
+                    j->busy = 1;
+                }
+                progressed = 1;
+            } else if (j->phase == PH_RUN) {
+                idle[n_idle++] = j;
             }
+        }
+        /* 2. quanta: least remaining work first (ties: arrival order), at
+         * most max_running jobs with work in flight */
+        for (unsigned int a = 1; a < n_idle; a++) {
+            job *k = idle[a];
+            const double rk = (double) (k->total_iters - k->done_iters) * k->work_per_iter;
+            unsigned int b = a;
+            while (b > 0) {
+                const job *p = idle[b - 1];
+                const double rp = (double) (p->total_iters - p->done_iters) * p->work_per_iter;
+                if (rp < rk || (rp == rk && p->id < k->id))
+                    break;
+                idle[b] = idle[b - 1];
+                b--;
+            }
+            idle[b] = k;
+        }
+        for (unsigned int i = 0; i < n_idle && running < max_running; i++) {
+            job *j = idle[i];
+            const int rc = job_quantum(s, j);
             if (rc != UFOIR_OK) {
                 j->phase = PH_END;
                 job_finish(s, j, rc);
             } else {
                 j->busy = 1;
+                running++;
             }
             progressed = 1;
         }
@@ -527,6 +576,7 @@ int ufoir_serve_submit(ufoir_server *s, const ufoir_job_desc *jd, const float *s
     j->user_sino = sino;
     j->user_vol = vol;
     j->bytes = job_bytes(jd);
+    j->work_per_iter = job_work_per_iter(jd);
     pthread_mutex_lock(&s->mu);
     if (s->stop) {
         pthread_mutex_unlock(&s->mu);

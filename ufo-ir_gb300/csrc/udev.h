@@ -78,9 +78,10 @@ int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, const float *
                   const float *src, const float *w, int w_shared, float *out, float scale, int n_slices);
 /* vol = vol + relax * A_angle^T sino (one-angle subset), in place; with
  * transposed != 0, vol holds the transpose of the volume. sn, cs: the
- * angle's entries of the float LUT. */
+ * angle's entries of the float LUT. relax_dev, if not NULL, replaces relax
+ * with the value it points to when the kernel runs. */
 int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino, float *vol,
-                  int transposed, float relax, int n_slices);
+                  int transposed, float relax, const float *relax_dev, int n_slices);
 
 /* ---- Tiled forward projector (all angles, shared-memory row streaming) ---- */
 /* Row pitch (floats, multiple of 4) of the padded images: 2 zero columns,
@@ -147,6 +148,27 @@ int udev_diff(udev *d, int which, const float *in, float *out, int w, int h, int
 /* sum |v| over each w*h slice, in the index order of ufo_ir_op_l1_norm. */
 int udev_l1_norm(udev *d, const float *v, size_t w, size_t h, int n_slices, int mode,
                  float *host_out);
+/* The same L1 norm into device memory (n_slices floats), with caller-owned
+ * FP64 partials (udev_l1_partials(n_slices) doubles; unused in COMPAT
+ * mode): no host synchronisation, capturable. */
+size_t udev_l1_partials(int n_slices);
+int udev_l1_norm_to(udev *d, const float *v, size_t w, size_t h, int n_slices, int mode, double *partials,
+                    float *d_out);
+
+/* ASD-POCS scalars in device memory (udev_asd.cu): beta, the SART
+ * relaxation and the outer-iteration count, and per slice the norms dp, dd,
+ * dg, l1 and the TV step dtgv. */
+typedef struct {
+    float *beta, *relax;
+    int *it;
+    float *dp, *dd, *dg, *dtgv, *l1;
+} udev_asd_scalars;
+int udev_asd_begin(udev *d, const udev_asd_scalars *S);
+int udev_asd_init(udev *d, const udev_asd_scalars *S, float alpha, int n_slices);
+int udev_asd_tv_step(udev *d, float *x, const float *grad, const udev_asd_scalars *S, size_t per_slice,
+                     int n_slices);
+int udev_asd_end(udev *d, const udev_asd_scalars *S, float beta_red, float r_max, float alpha_red, int n_slices);
+
 /* buggy-index dot product of ufo_ir_basic_ops_processor_dot_product. */
 int udev_dot(udev *d, const float *a, const float *b, size_t w, size_t h, int n_slices,
              int mode, float *host_out);

@@ -387,6 +387,31 @@ extern "C" int udev_l1_norm(udev *d, const float *v, size_t w, size_t h, int n_s
     return UFOIR_OK;
 }
 
+extern "C" size_t udev_l1_partials(int n_slices)
+{
+    return (size_t) kRedBlocks * (size_t) (n_slices > 0 ? n_slices : 0);
+}
+
+extern "C" int udev_l1_norm_to(udev *d, const float *v, size_t w, size_t h, int n_slices, int mode, double *partials,
+                               float *d_out)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    const size_t count = w * h;
+    int rc;
+    if (mode == UFOIR_NORM_COMPAT) {
+        l1_compat_kernel<<<n_slices, 32, 0, d->stream>>>(v, count, (long long) count, d_out);
+        return udev_after_launch(d, "l1_compat_kernel");
+    }
+    l1_fp64_partial_kernel<<<dim3(kRedBlocks, n_slices), kRedThreads, 0, d->stream>>>(v, count, (long long) count,
+                                                                                       partials);
+    if ((rc = udev_after_launch(d, "l1_fp64_partial_kernel")))
+        return rc;
+    sum_partials_kernel<<<n_slices, kRedThreads, 0, d->stream>>>(partials, kRedBlocks, d_out);
+    return udev_after_launch(d, "sum_partials_kernel");
+}
+
 extern "C" int udev_dot(udev *d, const float *a, const float *b, size_t w, size_t h, int n_slices,
                         int mode, float *host_out)
 {

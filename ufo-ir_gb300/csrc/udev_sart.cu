@@ -150,6 +150,7 @@ struct BpAngleArgs {
     float os, shift, e0, e1;   /* origin shift, os - ros, clamp edges (…joseph.cl:174-187) */
     float sn, cs;
     float relax;
+    const float *relax_dev;
     long long vol_stride;
     long long sino_stride;
 };
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
     if (j >= n)
         return;
     const float *r = P.sino + (size_t) slice * P.sino_stride + (size_t) P.angle * n;
+    const float relax = P.relax_dev ? *P.relax_dev : P.relax;
     const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
         const float sum =
             __fadd_rn(0.0f, joseph::lerp(t, joseph::texel(r, i0, n), joseph::texel(r, i0 + 1, n)));
         const size_t p = (size_t) slice * P.vol_stride + (size_t) j * n + i;
-        P.vol[p] = __fadd_rn(P.vol[p], __fmul_rn(P.relax, sum));
+        P.vol[p] = __fadd_rn(P.vol[p], __fmul_rn(relax, sum));
     }
 }
 
@@ -251,7 +253,7 @@ extern "C" int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, co
 }
 
 extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino,
-                             float *vol, int transposed, float relax, int n_slices)
+                             float *vol, int transposed, float relax, const float *relax_dev, int n_slices)
 {
     if (n_slices <= 0)
         return UFOIR_OK;
@@ -281,6 +283,7 @@ extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, f
     A.sn = sn;
     A.cs = cs;
     A.relax = relax;
+    A.relax_dev = relax_dev;
     A.vol_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
     dim3 grid(udev_div_up(n, 64), udev_div_up(n, 8), (unsigned int) n_slices);

@@ -87,7 +87,7 @@ class JobDesc(C.Structure):
 
 class ServeConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_uint), ("policy", C.c_int),
-                ("quantum", C.c_uint), ("fail_allocation_every", C.c_uint)]
+                ("quantum", C.c_uint), ("fail_allocation_every", C.c_uint), ("max_running", C.c_uint)]
 
 
 class ServeStats(C.Structure):
@@ -537,7 +537,8 @@ class Server:
     """The continuous-batching request loop (ufoir_serve_*)."""
 
     def __init__(self, ctx: Context, hbm_budget: int = 0, max_active_jobs: int = 0,
-                 policy: int = SERVE_CONTINUOUS, quantum: int = 1, fail_allocation_every: int = 0):
+                 policy: int = SERVE_CONTINUOUS, quantum: int = 1, fail_allocation_every: int = 0,
+                 max_running: int = 0):
         self.ctx = ctx
         cfg = ServeConfig()
         lib().ufoir_serve_config_init(C.byref(cfg))
@@ -547,6 +548,8 @@ class Server:
         cfg.policy = policy
         cfg.quantum = quantum
         cfg.fail_allocation_every = fail_allocation_every
+        if max_running:
+            cfg.max_running = max_running
         h = C.c_void_p()
         ctx._check(lib().ufoir_serve_create(ctx.handle, C.byref(cfg), C.byref(h)))
         self.handle = h.value
