@@ -159,13 +159,18 @@ def ncu_traffic():
     return {}
 
 
+def slice_seeds(rank, S):
+    """Phantom seeds of a rank's S slices: ranks reconstruct disjoint slices."""
+    return [2000 + rank * S + i for i in range(S)]
+
+
 def make_inputs(ufoir, ctx, proj, rank, S):
     """Phantoms -> Joseph FP on the GPU -> Poisson noise -> device sinograms."""
     from ufoir import synth
     n, na = N_DETS, N_ANGLES
     vols = np.empty((S, n, n), np.float32)
-    for i in range(S):
-        vols[i] = synth.ellipse_phantom(n, PHANTOM, 10, seed=2000 + rank * S + i)
+    for i, seed in enumerate(slice_seeds(rank, S)):
+        vols[i] = synth.ellipse_phantom(n, PHANTOM, 10, seed=seed)
     d_vol = ufoir.DeviceArray.from_numpy(ctx, vols)
     d_sino = ufoir.DeviceArray(ctx, (S, na, n), zero=True)
     proj.set(correction_scale=1.0, relaxation=1.0)
@@ -276,6 +281,7 @@ def run_ufoir(args, dist):
     serve = None
     if not args.quick and not args.no_serve and dist.rank == 0:
         serve = serve_section(ufoir, ctx)
+    methods = methods_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
 
     # roofline of the dominant kernel (live CUDA-event durations above)
     peak, peak_kind = measured_peaks()
@@ -313,6 +319,8 @@ def run_ufoir(args, dist):
            "kernel_ms": kernel_ms, "sample_rate": sample_rate, **per_job}
     if serve is not None:
         out["serve"] = serve
+    if methods is not None:
+        out["methods"] = methods
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and not args.quick:
         out["cpu_baseline"] = cpu_baseline(noisy[0])
     d_sino.close()
@@ -433,6 +441,52 @@ def serve_section(ufoir, ctx):
     return out
 
 
+# the other configured workloads: (name, method, n_dets, n_angles, phantom side, phantom kind, I0, params)
+METHOD_CASES = (
+    ("C1 SART 367^2 x 180 angles, 10 iterations", "sart", 367, 180, 256, "ellipses", None,
+     dict(num_iterations=10)),
+    ("C2 SIRT one slice 1448^2 x 1200 angles, 10 iterations", "sirt", 1448, 1200, 1024, "ellipses", 1e5,
+     dict(num_iterations=10)),
+    ("C3a ASD-POCS 2900^2 x 90 angles, 1 outer iteration (inner SART 10)", "asdpocs", 2900, 90, 2048, "polygons",
+     1e4, dict(num_iterations=1)),
+    ("C3b ASD-POCS 2900^2 x 360 angles, 1 outer iteration (inner SART 10)", "asdpocs", 2900, 360, 2048,
+     "polygons", 1e4, dict(num_iterations=1)),
+    ("C4 SBTV 1448^2 x 720 angles, 1 outer iteration", "sbtv", 1448, 720, 1024, "ellipses", 1e5,
+     {"num_iterations": 1, "lambda": 0.05, "mu": 1.0}),
+)
+
+
+def methods_section(ufoir, ctx):
+    """One call of each other configured method workload on one slice,
+    resident in HBM: the call time (after one untimed call) and its rate."""
+    from ufoir import synth
+    out = []
+    for name, method, n, na, P, kind, i0, kw in METHOD_CASES:
+        step = float(np.float32(np.pi / na))
+        vol = synth.phantom_for(n, P, kind, seed=7000 + n + na)
+        proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=1)
+        sino = proj.forward(vol, np.zeros((na, n), np.float32))
+        proj.close()
+        if i0:
+            sino, _ = synth.poisson_noise(sino, i0, seed=8000 + n + na)
+        d_sino = ufoir.DeviceArray.from_numpy(ctx, sino.astype(np.float32))
+        d_vol = ufoir.DeviceArray(ctx, (n, n), zero=True)
+        proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=0)
+        fn = getattr(ufoir, method)
+        fn(proj, d_sino, d_vol, **kw)
+        ctx.synchronize()
+        ctx.timer_begin()
+        fn(proj, d_sino, d_vol, **kw)
+        ms = ctx.timer_end()
+        iters = kw["num_iterations"]
+        out.append({"workload": name, "ms_per_call": ms, "ms_per_iteration": ms / iters,
+                    "samples_per_iteration_fp_bp": 2.0 * n * n * na})
+        proj.close()
+        d_sino.close()
+        d_vol.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -444,6 +498,8 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="only the resident timed steps (skip e2e, per-job comparison, serve trace, CPU baseline)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serve trace")
+    ap.add_argument("--methods", action="store_true",
+                    help="also time one call of each other configured method workload (C1, C2, C3a/b, C4)")
     args = ap.parse_args()
     dist = Dist()
     try:
