@@ -57,7 +57,8 @@ typedef enum {
     UFOIR_ERR_TIMEOUT = -6,      /* a bounded wait ran out */
     UFOIR_ERR_CANCELLED = -7,    /* job cancelled */
     UFOIR_ERR_STATE = -8,        /* object used in the wrong state */
-    UFOIR_ERR_NOT_FOUND = -9     /* unknown job id */
+    UFOIR_ERR_NOT_FOUND = -9,    /* unknown job id */
+    UFOIR_ERR_IO = -10           /* a file could not be read, parsed or written */
 } ufoir_status;
 
 /* ------------------------------------------------------------------------ */
@@ -290,7 +291,8 @@ UFOIR_API void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b);
 /* not depend on what else is in flight. Policy ONE_AT_A_TIME admits one    */
 /* job at a time (the plain per-job path) for comparison.                   */
 /* ------------------------------------------------------------------------ */
-enum { UFOIR_METHOD_SART = 0, UFOIR_METHOD_SIRT = 1, UFOIR_METHOD_ASDPOCS = 2 };
+/* Methods of a job or graph; the serve loop runs SART, SIRT and ASD-POCS. */
+enum { UFOIR_METHOD_SART = 0, UFOIR_METHOD_SIRT = 1, UFOIR_METHOD_ASDPOCS = 2, UFOIR_METHOD_SBTV = 3 };
 enum {
     UFOIR_JOB_QUEUED = 0,
     UFOIR_JOB_RUNNING = 1,
@@ -398,6 +400,63 @@ UFOIR_API int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, 
 #define UFOIR_NOALLOC_MAX_SLICES 64
 UFOIR_API int ufoir_l1_norm_fp64_noalloc(const float *d_v, size_t count, unsigned int n_slices,
                                          float *d_out, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Graphs in ufo-core's JSON format (json-sample.json): a "read" node, one  */
+/* ufo-ir method node of package "ir" (sart, sirt, asdpocs, sbtv) with its  */
+/* "projector" object (and ASD-POCS's "df_minimizer" SART object), and a    */
+/* "write" node, joined by edges read -> method -> write. Property names    */
+/* follow GObject: '-' and '_' are the same character. Values are checked   */
+/* against the property ranges above; an unknown property, plugin or        */
+/* package is an error (UFOIR_ERR_INVALID / UFOIR_ERR_UNSUPPORTED), with a   */
+/* message in err. Replaces ufo_plugin_manager + ufo_task_graph_read_from_  */
+/* file for these nodes (ufo-core; the reference's graphs use it through    */
+/* ufo-launch / ufo-runjson).                                              */
+/* Extension (no counterpart in the reference): a method node may set      */
+/* "norm-mode": "compat" | "fp64" for ASD-POCS and SBTV.                    */
+/* ------------------------------------------------------------------------ */
+#define UFOIR_PATH_MAX 1024
+typedef struct {
+    int method;                          /* UFOIR_METHOD_* */
+    ufoir_projector_params projector;    /* the method's "projector" node */
+    ufoir_sart_params sart;              /* SART / SIRT node */
+    ufoir_asdpocs_params asdpocs;        /* ASD-POCS node (df_minimizer inside) */
+    ufoir_sbtv_params sbtv;              /* SBTV node */
+    char read_path[UFOIR_PATH_MAX];      /* "read": "path" (a file or a glob pattern); "" = none */
+    unsigned int read_raw_width;         /* "read": "raw-width", "raw-height", "raw-offset" for  */
+    unsigned int read_raw_height;        /*   raw float32 files (0 = the file is a TIFF)        */
+    uint64_t read_raw_offset;
+    char write_filename[UFOIR_PATH_MAX]; /* "write": "filename" (printf counter, e.g. out%03i.tif); "" = none */
+} ufoir_graph;
+
+UFOIR_API int ufoir_graph_parse(const char *json, size_t len, ufoir_graph *out, char *err, size_t errlen);
+UFOIR_API int ufoir_graph_load(const char *path, ufoir_graph *out, char *err, size_t errlen);
+/* The job description of a graph's method node for a sinogram of n_dets x
+ * n_angles (SART, SIRT, ASD-POCS; SBTV gives UFOIR_ERR_UNSUPPORTED). */
+UFOIR_API int ufoir_graph_job_desc(const ufoir_graph *g, unsigned int n_dets, unsigned int n_angles,
+                                   ufoir_job_desc *out);
+/* Runs a graph: reads every sinogram slice of read_path (TIFF pages, or raw
+ * float32 slices of raw-width x raw-height), reconstructs them with the
+ * method node, and writes the volumes to write_filename: one file per slice
+ * when it holds a printf counter (counter from 0), else one multi-page TIFF.
+ * *n_slices (may be NULL) receives the number of slices written. */
+UFOIR_API int ufoir_graph_run(ufoir_ctx *ctx, const ufoir_graph *g, unsigned int *n_slices);
+
+/* ------------------------------------------------------------------------ */
+/* Slice files at the graph's edges (the reference's graphs use ufo-filters' */
+/* read/write plugins): classic TIFF with 32-bit float, 16-bit or 8-bit      */
+/* unsigned samples, one sample per pixel, uncompressed strips, either byte  */
+/* order (read; written little-endian float32), one slice per page; raw      */
+/* float32 in host byte order. Errors return UFOIR_ERR_IO (or _INVALID) with */
+/* a message in ufoir_io_last_error() (per thread).                          */
+/* ------------------------------------------------------------------------ */
+UFOIR_API const char *ufoir_io_last_error(void);
+UFOIR_API int ufoir_io_tiff_info(const char *path, unsigned int *width, unsigned int *height, unsigned int *pages);
+UFOIR_API int ufoir_io_read_tiff(const char *path, unsigned int page, float *out, size_t count);
+UFOIR_API int ufoir_io_write_tiff(const char *path, const float *data, unsigned int width, unsigned int height,
+                                  unsigned int pages);
+UFOIR_API int ufoir_io_read_raw(const char *path, uint64_t offset, float *out, size_t count);
+UFOIR_API int ufoir_io_write_raw(const char *path, const float *data, size_t count);
 
 #ifdef __cplusplus
 }

@@ -30,6 +30,7 @@ ERR_TIMEOUT = -6
 ERR_CANCELLED = -7
 ERR_STATE = -8
 ERR_NOT_FOUND = -9
+ERR_IO = -10
 
 HORIZONTAL = 0
 VERTICAL = 1
@@ -75,6 +76,16 @@ class SbtvParams(C.Structure):
 METHOD_SART = 0
 METHOD_SIRT = 1
 METHOD_ASDPOCS = 2
+METHOD_SBTV = 3
+PATH_MAX = 1024
+
+
+class Graph(C.Structure):
+    """ufoir_graph: a parsed ufo-core JSON graph (read -> method -> write)."""
+    _fields_ = [("method", C.c_int), ("projector", ProjectorParams), ("sart", SartParams),
+                ("asdpocs", AsdpocsParams), ("sbtv", SbtvParams), ("read_path", C.c_char * PATH_MAX),
+                ("read_raw_width", C.c_uint), ("read_raw_height", C.c_uint), ("read_raw_offset", C.c_uint64),
+                ("write_filename", C.c_char * PATH_MAX)]
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = 0, 1, 2, 3, 4
 SERVE_CONTINUOUS = 0
 SERVE_ONE_AT_A_TIME = 1
@@ -121,7 +132,9 @@ EXPORTED = (
     "ufoir_sirt_batch_profile", "ufoir_sirt_batch_destroy", "ufoir_ctx_timer_begin",
     "ufoir_ctx_timer_end", "ufoir_serve_config_init", "ufoir_job_desc_init", "ufoir_serve_create",
     "ufoir_serve_submit", "ufoir_serve_poll", "ufoir_serve_wait", "ufoir_serve_cancel", "ufoir_serve_drain",
-    "ufoir_serve_get_stats", "ufoir_serve_destroy",
+    "ufoir_serve_get_stats", "ufoir_serve_destroy", "ufoir_graph_parse", "ufoir_graph_load",
+    "ufoir_graph_job_desc", "ufoir_graph_run", "ufoir_io_last_error", "ufoir_io_tiff_info", "ufoir_io_read_tiff",
+    "ufoir_io_write_tiff", "ufoir_io_read_raw", "ufoir_io_write_raw",
 )
 
 
@@ -199,6 +212,17 @@ def _declare(L):
     L.ufoir_serve_get_stats.argtypes = [vp, C.POINTER(ServeStats)]
     L.ufoir_serve_destroy.argtypes = [vp]
     L.ufoir_serve_destroy.restype = None
+    L.ufoir_graph_parse.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(Graph), C.c_char_p, C.c_size_t]
+    L.ufoir_graph_load.argtypes = [C.c_char_p, C.POINTER(Graph), C.c_char_p, C.c_size_t]
+    L.ufoir_graph_job_desc.argtypes = [C.POINTER(Graph), C.c_uint, C.c_uint, C.POINTER(JobDesc)]
+    L.ufoir_graph_run.argtypes = [vp, C.POINTER(Graph), C.POINTER(C.c_uint)]
+    L.ufoir_io_last_error.argtypes = []
+    L.ufoir_io_last_error.restype = C.c_char_p
+    L.ufoir_io_tiff_info.argtypes = [C.c_char_p, C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
+    L.ufoir_io_read_tiff.argtypes = [C.c_char_p, C.c_uint, vp, C.c_size_t]
+    L.ufoir_io_write_tiff.argtypes = [C.c_char_p, vp, C.c_uint, C.c_uint, C.c_uint]
+    L.ufoir_io_read_raw.argtypes = [C.c_char_p, C.c_uint64, vp, C.c_size_t]
+    L.ufoir_io_write_raw.argtypes = [C.c_char_p, vp, C.c_size_t]
     L.ufoir_l1_norm.argtypes = [vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
     L.ufoir_dot_product.argtypes = [vp, vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
 
@@ -597,3 +621,76 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+# ---------------------------------------------------------------- graphs, I/O
+
+def graph_parse(text: str) -> Graph:
+    """Parse a ufo-core JSON graph (read -> ufo-ir method -> write)."""
+    g = Graph()
+    err = C.create_string_buffer(512)
+    b = text.encode()
+    rc = lib().ufoir_graph_parse(b, len(b), C.byref(g), err, len(err))
+    if rc != OK:
+        raise UfoirError(rc, err.value.decode())
+    return g
+
+
+def graph_load(path: str) -> Graph:
+    g = Graph()
+    err = C.create_string_buffer(512)
+    rc = lib().ufoir_graph_load(path.encode(), C.byref(g), err, len(err))
+    if rc != OK:
+        raise UfoirError(rc, err.value.decode())
+    return g
+
+
+def graph_job_desc(g: Graph, n_dets: int, n_angles: int) -> JobDesc:
+    j = JobDesc()
+    rc = lib().ufoir_graph_job_desc(C.byref(g), n_dets, n_angles, C.byref(j))
+    if rc != OK:
+        raise UfoirError(rc, "graph_job_desc")
+    return j
+
+
+def graph_run(ctx: Context, g: Graph) -> int:
+    """Read, reconstruct and write every slice of a parsed graph; returns the slice count."""
+    n = C.c_uint()
+    ctx._check(lib().ufoir_graph_run(ctx.handle, C.byref(g), C.byref(n)))
+    return n.value
+
+
+def _io_check(rc):
+    if rc != OK:
+        raise UfoirError(rc, lib().ufoir_io_last_error().decode())
+
+
+def tiff_info(path: str):
+    w, h, p = C.c_uint(), C.c_uint(), C.c_uint()
+    _io_check(lib().ufoir_io_tiff_info(path.encode(), C.byref(w), C.byref(h), C.byref(p)))
+    return w.value, h.value, p.value
+
+
+def read_tiff(path: str, page: int = 0) -> np.ndarray:
+    w, h, _ = tiff_info(path)
+    out = np.empty((h, w), np.float32)
+    _io_check(lib().ufoir_io_read_tiff(path.encode(), page, out.ctypes.data, out.size))
+    return out
+
+
+def write_tiff(path: str, data: np.ndarray):
+    """data: (h, w) or (pages, h, w) float32."""
+    a = np.ascontiguousarray(data, np.float32)
+    pages = 1 if a.ndim == 2 else a.shape[0]
+    _io_check(lib().ufoir_io_write_tiff(path.encode(), a.ctypes.data, a.shape[-1], a.shape[-2], pages))
+
+
+def read_raw(path: str, shape, offset: int = 0) -> np.ndarray:
+    out = np.empty(shape, np.float32)
+    _io_check(lib().ufoir_io_read_raw(path.encode(), offset, out.ctypes.data, out.size))
+    return out
+
+
+def write_raw(path: str, data: np.ndarray):
+    a = np.ascontiguousarray(data, np.float32)
+    _io_check(lib().ufoir_io_write_raw(path.encode(), a.ctypes.data, a.size))
