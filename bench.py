@@ -300,9 +300,16 @@ def run_ufoir(args, dist):
                 "algorithmic_bytes_per_launch": dom_bytes,
                 "note": "compulsory bytes / kernel time; the projectors are bound by interpolated-sample "
                         "issue, not HBM, so this fraction is small by construction"}
-    sample_rate = {"fp_samples_per_s": fp_samples / (kernel_ms["fp"] / 1e3),
-                   "bp_samples_per_s": bp_samples / (kernel_ms["bp"] / 1e3),
-                   "fp_samples_per_launch": fp_samples, "bp_samples_per_launch": bp_samples}
+    ceiling = ctx.sample_ceiling()
+    fp_rate = fp_samples / (kernel_ms["fp"] / 1e3)
+    bp_rate = bp_samples / (kernel_ms["bp"] / 1e3)
+    sample_rate = {"fp_samples_per_s": fp_rate, "bp_samples_per_s": bp_rate,
+                   "fp_samples_per_launch": fp_samples, "bp_samples_per_launch": bp_samples,
+                   "ceiling_samples_per_s": ceiling,
+                   "fp_frac": fp_rate / ceiling if ceiling else None,
+                   "bp_frac": bp_rate / ceiling if ceiling else None,
+                   "ceiling": "measured in this run (ufoir_sample_ceiling): the FP's exact per-sample "
+                              "sequence from shared memory on every SM, no global traffic"}
 
     out = {"metric": METRIC, "value": value, "unit": "slice-iters/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,

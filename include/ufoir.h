@@ -397,6 +397,12 @@ UFOIR_API int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, 
 /* the default stream) and d_out is valid once the stream reaches it. No   */
 /* cudaMalloc, cudaFree or allocating library call is made.                 */
 /* ------------------------------------------------------------------------ */
+/* Measurement (no counterpart in the reference): the interpolated-sample  */
+/* rate ceiling of the device, i.e. the forward projector's exact per-      */
+/* sample instruction sequence run from shared memory by every SM with no   */
+/* global traffic. Projector sample rates are reported against it.          */
+UFOIR_API int ufoir_sample_ceiling(ufoir_ctx *ctx, double *samples_per_s);
+
 #define UFOIR_NOALLOC_MAX_SLICES 64
 UFOIR_API int ufoir_l1_norm_fp64_noalloc(const float *d_v, size_t count, unsigned int n_slices,
                                          float *d_out, void *stream);

@@ -183,3 +183,10 @@ void ufoir__buf_release(ufoir_ctx *ctx, ufoir_buf *b)
     b->dev = NULL;
     b->owned = 0;
 }
+
+int ufoir_sample_ceiling(ufoir_ctx *ctx, double *samples_per_s)
+{
+    if (!ctx || !samples_per_s)
+        return UFOIR_ERR_INVALID;
+    return udev_sample_ceiling(ctx->dev, samples_per_s);
+}

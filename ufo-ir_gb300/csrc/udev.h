@@ -66,6 +66,10 @@ int udev_fp(udev *d, const udev_geom *g, int a0, int na, int dir_override,
 /* Transpose n x n slices. */
 int udev_transpose(udev *d, const float *in, float *out, int n, int n_slices);
 
+/* Interpolated samples/s of the forward projector's per-sample sequence run
+ * from shared memory on every SM with no global traffic (udev_ceiling.cu). */
+int udev_sample_ceiling(udev *d, double *samples_per_s);
+
 /* ---- Per-angle projections of a SART sweep (udev_sart.cu) ---- */
 /* Floats of the block-start table: the coordinate of every ray of every
  * angle at the start of each 64-sample block, [n_angles][ceil(n/64)][n]. */
