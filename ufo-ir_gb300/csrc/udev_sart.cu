@@ -29,8 +29,7 @@ namespace {
 constexpr int kBlock = 64;          /* samples per block (the reference's BLOCK_SIZE) */
 constexpr int kRaysPerCta = 8;      /* lanes: 8 rays x 4 blocks per warp */
 constexpr int kMaxBlocks = 128;     /* n <= 8192 */
-constexpr int kGroup = 16;          /* samples whose loads are issued together */
-constexpr int kMaxThreads = 512;
+constexpr int kMaxThreads = 512;          /* 16 warps: blocks beyond them loop */
 
 __global__ void __launch_bounds__(256) block_starts_kernel(const float *__restrict__ sinv,
                                                            const float *__restrict__ cosv,
@@ -73,56 +72,74 @@ struct FpAngleArgs {
     long long w_stride;
 };
 
-/* out = (src + scale * S) [* w] for the rays of one angle. Grid
- * (ceil(n / 8), slices); block 32 * min(16, ceil(n_blocks / 4)) threads,
- * thread (ray, b0) taking blocks b0, b0 + blockDim / 8, ... */
+/*
+ * out = (src + scale * S) [* w] for the rays of one angle.
+ *
+ * A warp takes one 64-sample block of 8 adjacent rays; lane = 8 * q + ray,
+ * and quarter q computes samples 16q .. 16q + 15 of the block. The quarter's
+ * start coordinate is the block start (table) advanced by 16q steps of the
+ * same float recurrence. The 16 sample values are computed independently
+ * (all loads in flight together); the block's in-order sum is then folded
+ * through the quarters with shuffles, so the additions happen in exactly the
+ * reference's order. Samples in rows >= n read the zero border and add 0,
+ * as in the reference's fixed 64-sample blocks.
+ * Grid (ceil(n / 8), slices); block 32 * min(kMaxWarps, n_blocks) threads.
+ */
 __global__ void __launch_bounds__(kMaxThreads) fp_angle_kernel(FpAngleArgs P)
 {
     __shared__ float bsum[kMaxBlocks][kRaysPerCta];
     const int lane = (int) (threadIdx.x & 31);
     const int ray = lane & (kRaysPerCta - 1);
+    const int q = lane >> 3;
     const int s = (int) blockIdx.x * kRaysPerCta + ray;
+    const int sc = min(s, P.n - 1);          /* lanes past the last ray compute a copy and write nothing */
     const int slice = (int) blockIdx.y;
     const int n = P.n;
+    float det_step, step;
+    joseph::ray_steps(P.dir, P.sinv[P.angle], P.cosv[P.angle], det_step, step);
+    const float *img = P.img + (size_t) slice * P.img_stride;
 
-    for (int b = (int) (threadIdx.x >> 5) * 4 + (lane >> 3); s < n && b < P.n_blocks;
-         b += (int) blockDim.x / kRaysPerCta) {
-        float det_step, step;
-        joseph::ray_steps(P.dir, P.sinv[P.angle], P.cosv[P.angle], det_step, step);
-        const float *img = P.img + (size_t) slice * P.img_stride;
-        float c = P.table[((size_t) P.angle * P.n_blocks + b) * n + s];
-        const int row0 = b * kBlock;
-        const int rows = min(kBlock, n - row0);
-        const float *row = img + (size_t) row0 * n;
-        float inner = 0.0f;
-        /* Groups of kGroup samples: the coordinates first (the float
-         * recurrence), then all loads (unconditional, indices clamped into
-         * the row; the zero border is applied afterwards), then the in-order
-         * sum, so that 2 * kGroup loads are in flight per thread. */
-        for (int g0 = 0; g0 < rows; g0 += kGroup) {
-            int i0[kGroup];
-            float t[kGroup], va[kGroup], vb[kGroup];
+    for (int b = (int) (threadIdx.x >> 5); b < P.n_blocks; b += (int) (blockDim.x >> 5)) {
+        float c = P.table[((size_t) P.angle * P.n_blocks + b) * n + sc];
+        for (int k = 0; k < 16 * q; ++k)
+            c = __fadd_rn(c, step);
+        const int row0 = b * kBlock + 16 * q;
+        int i0[16];
+        float t[16], va[16], vb[16];
 #pragma unroll
-            for (int k = 0; k < kGroup; ++k) {
-                joseph::lerp_coord(c, i0[k], t[k]);
-                c = __fadd_rn(c, step);
-            }
-#pragma unroll
-            for (int k = 0; k < kGroup; ++k) {
-                const float *rr = row + (size_t) min(g0 + k, rows - 1) * n;
-                va[k] = __ldg(rr + min(max(i0[k], 0), n - 1));
-                vb[k] = __ldg(rr + min(max(i0[k] + 1, 0), n - 1));
-            }
-#pragma unroll
-            for (int k = 0; k < kGroup; ++k) {
-                if (g0 + k < rows) {
-                    const float t0 = (unsigned) i0[k] < (unsigned) n ? va[k] : 0.0f;
-                    const float t1 = (unsigned) (i0[k] + 1) < (unsigned) n ? vb[k] : 0.0f;
-                    inner = __fadd_rn(inner, joseph::lerp(t[k], t0, t1));
-                }
-            }
+        for (int k = 0; k < 16; ++k) {
+            joseph::lerp_coord(c, i0[k], t[k]);
+            c = __fadd_rn(c, step);
         }
-        bsum[b][ray] = inner;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const float *rr = img + (size_t) min(row0 + k, n - 1) * n;
+            va[k] = __ldg(rr + min(max(i0[k], 0), n - 1));
+            vb[k] = __ldg(rr + min(max(i0[k] + 1, 0), n - 1));
+        }
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const bool in_row = row0 + k < n;
+            const float t0 = in_row && (unsigned) i0[k] < (unsigned) n ? va[k] : 0.0f;
+            const float t1 = in_row && (unsigned) (i0[k] + 1) < (unsigned) n ? vb[k] : 0.0f;
+            v[k] = joseph::lerp(t[k], t0, t1);
+        }
+        /* inner = (((0 + v_0) + v_1) + ... + v_63), quarter by quarter */
+        float run = 0.0f;
+#pragma unroll
+        for (int stage = 0; stage < 4; ++stage) {
+            if (q == stage) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k)
+                    run = __fadd_rn(run, v[k]);
+            }
+            const float from_prev = __shfl_up_sync(0xffffffffu, run, kRaysPerCta);
+            if (q == stage + 1)
+                run = from_prev;
+        }
+        if (q == 3)
+            bsum[b][ray] = run;
     }
     __syncthreads();
     if (threadIdx.x < kRaysPerCta && s < n) {
@@ -156,23 +173,37 @@ struct BpAngleArgs {
 };
 
 /* vol = vol + relax * (0 + sample) for one angle (…joseph.cl:158-218 with a
- * one-angle subset). Grid (ceil(n / 64), ceil(n / 8), slices), block 32 x 8;
- * a thread updates storage columns i and i + 32 of one storage row. */
+ * one-angle subset). Grid (ceil(n / 128), ceil(n / 8), slices), block 32 x 8;
+ * a thread updates 4 consecutive storage columns of one storage row, with
+ * 16-byte loads and stores when rows are 16-byte aligned (VEC). */
+template <bool VEC>
 __global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
 {
     const int j = (int) (blockIdx.y * blockDim.y + threadIdx.y);   /* storage row */
+    const int i_first = (int) (blockIdx.x * blockDim.x + threadIdx.x) * 4;
     const int slice = (int) blockIdx.z;
     const int n = P.n;
-    if (j >= n)
+    if (j >= n || i_first >= n)
         return;
     const float *r = P.sino + (size_t) slice * P.sino_stride + (size_t) P.angle * n;
     const float relax = P.relax_dev ? *P.relax_dev : P.relax;
     const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
+    float *row = P.vol + (size_t) slice * P.vol_stride + (size_t) j * n;
+    float v[4];
+    if (VEC) {
+        const float4 x4 = *reinterpret_cast<const float4 *>(row + i_first);
+        v[0] = x4.x;
+        v[1] = x4.y;
+        v[2] = x4.z;
+        v[3] = x4.w;
+    } else {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int i = (int) (blockIdx.x * 64 + threadIdx.x) + 32 * h;   /* storage column */
-        if (i >= n)
-            break;
+        for (int h = 0; h < 4; ++h)
+            v[h] = i_first + h < n ? row[i_first + h] : 0.0f;
+    }
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        const int i = i_first + h;   /* storage column */
         const float fI = __fsub_rn(__fadd_rn((float) i, 0.5f), P.os);
         const float fX = P.transposed ? fJ : fI;
         const float fY = P.transposed ? fI : fJ;
@@ -186,8 +217,15 @@ __global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
         joseph::lerp_coord(sc, i0, t);
         const float sum =
             __fadd_rn(0.0f, joseph::lerp(t, joseph::texel(r, i0, n), joseph::texel(r, i0 + 1, n)));
-        const size_t p = (size_t) slice * P.vol_stride + (size_t) j * n + i;
-        P.vol[p] = __fadd_rn(P.vol[p], __fmul_rn(relax, sum));
+        v[h] = __fadd_rn(v[h], __fmul_rn(relax, sum));
+    }
+    if (VEC) {
+        *reinterpret_cast<float4 *>(row + i_first) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+            if (i_first + h < n)
+                row[i_first + h] = v[h];
     }
 }
 
@@ -245,8 +283,8 @@ extern "C" int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, co
     A.img_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
     A.w_stride = w_shared ? 0 : A.sino_stride;
-    const int warps = (A.n_blocks + 3) / 4;
-    const int threads = 32 * (warps < kMaxThreads / 32 ? warps : kMaxThreads / 32);
+    const int warps = A.n_blocks < kMaxThreads / 32 ? A.n_blocks : kMaxThreads / 32;
+    const int threads = 32 * warps;
     dim3 grid(udev_div_up(n, kRaysPerCta), (unsigned int) n_slices);
     fp_angle_kernel<<<grid, threads, 0, d->stream>>>(A);
     return udev_after_launch(d, "fp_angle_kernel");
@@ -286,7 +324,11 @@ extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, f
     A.relax_dev = relax_dev;
     A.vol_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
-    dim3 grid(udev_div_up(n, 64), udev_div_up(n, 8), (unsigned int) n_slices);
-    bp_angle_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    dim3 grid(udev_div_up(n, 128), udev_div_up(n, 8), (unsigned int) n_slices);
+    const bool vec = (n % 4) == 0 && (reinterpret_cast<uintptr_t>(vol) & 15) == 0;
+    if (vec)
+        bp_angle_kernel<true><<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    else
+        bp_angle_kernel<false><<<grid, dim3(32, 8), 0, d->stream>>>(A);
     return udev_after_launch(d, "bp_angle_kernel");
 }
