@@ -205,6 +205,21 @@ def test_full_size_bp_matches_oracle_on_a_row_band(ufoir_lib, gpu_ctx, oracle):
     assert rel_l2(gb, wb) <= TOL_ONE and np.array_equal(gb, wb)
 
 
+@pytest.mark.parametrize("n,na,axis,slices", [(1448, 48, -1.0, 1), (1448, 48, 700.3, 1), (1000, 40, -1.0, 3)])
+def test_fp_with_few_tiles_splits_detectors(ufoir_lib, gpu_ctx, oracle, n, na, axis, slices):
+    # few angles on few slices leave most SMs without an angle tile, so each
+    # tile's detectors are spread over several CTAs; results must not change
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(n + na + slices)
+    vols = rng.random((slices, n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, axis)
+    got = p.forward(vols, np.zeros((slices, na, n), np.float32))
+    op = oracle.projector(n, na, step, axis)
+    for i in range(slices):
+        want = oracle.forward(op, vols[i])
+        assert rel_l2(got[i], want) <= TOL_ONE and np.array_equal(got[i], want)
+
+
 def test_errors_are_reported_not_fatal(ufoir_lib, gpu_ctx):
     with pytest.raises(ufoir_lib.UfoirError) as e:
         ufoir_lib.ParallelProjector(gpu_ctx, model="siddon")

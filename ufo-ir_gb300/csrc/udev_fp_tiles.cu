@@ -51,6 +51,8 @@ struct FpTileArgs {
     long long sino_stride;
     long long w_stride;
     float neg_zero;        /* -0.0f: the addend of unfusable packed products */
+    int dsplit;            /* CTAs per angle tile, each on a range of dper detectors */
+    int dper;
     int *err;
 };
 
@@ -64,10 +66,13 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
     const int pitch = P.pitch;
     const size_t stage_floats = (size_t) K * pitch;
 
-    const int4 tile = P.tiles[blockIdx.x];
+    const int4 tile = P.tiles[blockIdx.x / (unsigned) P.dsplit];
     const int slice = (int) blockIdx.y;
     const int n = P.n;
     const int dir = tile.z;
+    /* detector range of this CTA: [dstart, dend) */
+    const int dstart = (int) (blockIdx.x % (unsigned) P.dsplit) * P.dper;
+    const int dend = min(n, dstart + P.dper);
     const float *img = (dir == 0 ? P.volTP : P.volP) + (size_t) slice * P.volp_stride;
 
     const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
@@ -82,7 +87,7 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
     const int lane = (int) (threadIdx.x & 31);
     const int g = lane >> 4;
     const int half = (int) (blockDim.x >> 1);
-    const int d0 = (int) (threadIdx.x >> 5) * 16 + (lane & 15);
+    const int d0 = dstart + (int) (threadIdx.x >> 5) * 16 + (lane & 15);
     float2 c[A2][J], inner[A2][J], sum[A2][J], stp[A2];
 #pragma unroll
     for (int k = 0; k < A2; ++k) {
@@ -96,8 +101,8 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
 #pragma unroll
         for (int m = 0; m < J; ++m) {
             const int s0 = d0 + 2 * m * half, s1 = s0 + half;
-            c[k][m] = make_float2((a < tile.y && s0 < n) ? joseph::ray_start(kc, s0, n, det_step, st) : 0.0f,
-                                  (a < tile.y && s1 < n) ? joseph::ray_start(kc, s1, n, det_step, st) : 0.0f);
+            c[k][m] = make_float2((a < tile.y && s0 < dend) ? joseph::ray_start(kc, s0, n, det_step, st) : 0.0f,
+                                  (a < tile.y && s1 < dend) ? joseph::ray_start(kc, s1, n, det_step, st) : 0.0f);
             inner[k][m] = make_float2(0.0f, 0.0f);
             sum[k][m] = make_float2(0.0f, 0.0f);
         }
@@ -203,7 +208,7 @@ __global__ void __launch_bounds__(768, 1) fp_tiles_kernel(FpTileArgs P)
 #pragma unroll
         for (int i = 0; i < 2 * J; ++i) {
             const int s = d0 + i * half;
-            if (s >= n)
+            if (s >= dend)
                 continue;
             const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + s;
             float result = P.src[oidx];
@@ -268,7 +273,7 @@ TileCfg tile_cfg(int n, int smem_optin)
 }
 
 template <int J, int A>
-int launch_tiles(udev *d, const FpTileArgs &args, int n_tiles, int n_slices, const TileCfg &cfg)
+int launch_tiles(udev *d, const FpTileArgs &args, int n_tiles, int n_slices, int threads, size_t smem)
 {
     for (int done = 0; done < n_slices;) {
         const int chunk = n_slices - done > 65535 ? 65535 : n_slices - done;
@@ -279,7 +284,7 @@ int launch_tiles(udev *d, const FpTileArgs &args, int n_tiles, int n_slices, con
         B.out += (size_t) done * args.sino_stride;
         if (B.w)
             B.w += (size_t) done * args.w_stride;
-        fp_tiles_kernel<J, A><<<dim3((unsigned int) n_tiles, (unsigned int) chunk), cfg.threads, cfg.smem,
+        fp_tiles_kernel<J, A><<<dim3((unsigned int) (n_tiles * args.dsplit), (unsigned int) chunk), threads, smem,
                                 d->stream>>>(B);
         int rc = udev_after_launch(d, "fp_tiles_kernel");
         if (rc)
@@ -372,11 +377,37 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
     A.w_stride = w_shared ? 0 : A.sino_stride;
     A.neg_zero = -0.0f;
     A.err = d->d_err;
+    /* Too few tiles to fill the GPU (one slice, few angles): split each
+     * angle tile's detectors over up to 8 CTAs, with chunks small enough
+     * for two CTAs per SM. Every CTA still walks all rows; only L2 reads of
+     * the image grow. */
+    int threads = cfg.threads, K = cfg.K;
+    A.dsplit = 1;
+    A.dper = n;
+    const long long ctas = (long long) n_tiles * n_slices;
+    if (ctas < d->sm_count) {
+        int split = (int) ((2LL * d->sm_count + ctas - 1) / ctas);
+        split = split > 8 ? 8 : split;
+        while (split > 1 && (n + split - 1) / split < 64)
+            split--;
+        int k2 = K;
+        while (k2 > 4 && 2 * (128 + 2 * (size_t) k2 * A.pitch * 4) > (size_t) d->smem_optin)
+            k2 /= 2;
+        if (split > 1 && 2 * (128 + 2 * (size_t) k2 * A.pitch * 4) <= (size_t) d->smem_optin) {
+            A.dsplit = split;
+            A.dper = (n + split - 1) / split;
+            const int slots = (A.dper + 2 * cfg.J - 1) / (2 * cfg.J);
+            threads = (slots + 15) / 16 * 32;
+            K = k2;
+        }
+    }
+    A.rows_per_chunk = K;
+    const size_t smem = 128 + 2 * (size_t) K * A.pitch * 4;
     switch (cfg.J * 16 + cfg.A) {
-    case 1 * 16 + 8: return launch_tiles<1, 8>(d, A, n_tiles, n_slices, cfg);
-    case 2 * 16 + 8: return launch_tiles<2, 8>(d, A, n_tiles, n_slices, cfg);
-    case 4 * 16 + 4: return launch_tiles<4, 4>(d, A, n_tiles, n_slices, cfg);
-    case 8 * 16 + 2: return launch_tiles<8, 2>(d, A, n_tiles, n_slices, cfg);
+    case 1 * 16 + 8: return launch_tiles<1, 8>(d, A, n_tiles, n_slices, threads, smem);
+    case 2 * 16 + 8: return launch_tiles<2, 8>(d, A, n_tiles, n_slices, threads, smem);
+    case 4 * 16 + 4: return launch_tiles<4, 4>(d, A, n_tiles, n_slices, threads, smem);
+    case 8 * 16 + 2: return launch_tiles<8, 2>(d, A, n_tiles, n_slices, threads, smem);
     default:
         udev_set_error(d, "fp_tiles: no kernel for J=%d A=%d", cfg.J, cfg.A);
         return UFOIR_ERR_UNSUPPORTED;
