@@ -61,6 +61,9 @@ struct BpTileArgs {
 struct __align__(16) BpSmem {
     float win[2][kAC][kWin];
     float4 ang[2][kAC];
+    /* (-fY) * sin for the tile's 64 rows, [angle][ty][pixel p of the
+     * thread's column, 4 per float4]: the same for all 32 lanes of a warp */
+    float4 nys[2][kAC][kTY][kPY / 4];
 };
 
 __device__ __forceinline__ void cp_async4(float *dst, const float *src)
@@ -137,6 +140,13 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
         S.ang[buf][tid] = make_float4(cs, sn, __int_as_float(w0), 0.0f);
     }
     __syncthreads();
+    /* row products of the chunk's angles, rounded as the in-loop product */
+    float *nys = reinterpret_cast<float *>(&S.nys[buf][0][0][0]);
+    for (int idx = tid; idx < count * kTileY; idx += kTX * kTY) {
+        const int slot = idx / kTileY, r = idx % kTileY;      /* row r = ty + kTY * p */
+        const float nfy = -__fsub_rn(__fadd_rn((float) (y0 + r), 0.5f), k.os);
+        nys[(slot * kTY + r % kTY) * kPY + r / kTY] = __fmul_rn(nfy, S.ang[buf][slot].y);
+    }
     constexpr int kGroups = kWin / 4;
     for (int idx = tid; idx < count * kGroups; idx += kTX * kTY) {
         const int slot = idx / kGroups, g = idx % kGroups;
@@ -165,7 +175,7 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
  */
 template <bool CLAMP, bool FAST>
 __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count, int first_vi, const BpTileArgs &P,
-                                             float fX, const float2 nfY[kPY / 2], float shift, float e0, float e1,
+                                             float fX, float shift, float e0, float e1,
                                              float2 sum[kPY / 2], float2 v[kPY / 2], int &sub, int &sub_end)
 {
     const uint32_t win0 = (uint32_t) __cvta_generic_to_shared(&S.win[buf][0][0]);
@@ -185,14 +195,16 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
             sub_end += (int) P.sub_n[sub];
         }
         const float4 ang = S.ang[buf][i];
+        const float4 ny0 = S.nys[buf][i][threadIdx.y][0], ny1 = S.nys[buf][i][threadIdx.y][1];
+        const float2 nys[kPY / 2] = {make_float2(ny0.x, ny0.y), make_float2(ny0.z, ny0.w), make_float2(ny1.x, ny1.y),
+                                     make_float2(ny1.z, ny1.w)};
         /* shared address of detector 0 of this angle's window, less the floor bits */
         const uint32_t base = win0 + 4u * (uint32_t) (i * kWin) - 4u * ((uint32_t) __float_as_int(ang.z) + bits);
         const float2 fxc = joseph::splat(__fmul_rn(fX, ang.x));
-        const float2 sn = joseph::splat(ang.y);
 #pragma unroll
         for (int q = 0; q < kPY / 2; ++q) {
             /* fX * cos - fY * sin + shift, as fX*cos + (-fY)*sin + shift */
-            float2 sc = joseph::add2(joseph::add2(fxc, joseph::mul2z(nfY[q], sn, z2)), shift2);
+            float2 sc = joseph::add2(joseph::add2(fxc, nys[q]), shift2);
             if (CLAMP) {
                 sc.x = fminf(fmaxf(sc.x, e0), e1);
                 sc.y = fminf(fmaxf(sc.y, e0), e1);
@@ -225,20 +237,17 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
 
     const int x = x0 + (int) threadIdx.x;
     const float fX = __fsub_rn(__fadd_rn((float) x, 0.5f), k.os);
-    /* pixel pairs (p, p + 1) of the thread's column; -fY so that the
-     * coordinate is fX*cos + (-fY)*sin + shift */
-    float2 nfY[kPY / 2], sum[kPY / 2], v[kPY / 2];
+    /* pixel pairs (p, p + 1) of the thread's column */
+    float2 sum[kPY / 2], v[kPY / 2];
 #pragma unroll
     for (int q = 0; q < kPY / 2; ++q) {
-        float f[2], b[2];
+        float b[2];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int y = y0 + (int) threadIdx.y + kTY * (2 * q + h);
-            f[h] = -__fsub_rn(__fadd_rn((float) y, 0.5f), k.os);
             const size_t pix = (size_t) slice * P.vol_stride + (size_t) y * n + x;
             b[h] = (P.base && x < n && y < n) ? P.base[pix] : 0.0f;
         }
-        nfY[q] = make_float2(f[0], f[1]);
         v[q] = make_float2(b[0], b[1]);
         sum[q] = make_float2(0.0f, 0.0f);
     }
@@ -276,11 +285,11 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
         __syncthreads();
         const int count = min(kAC, P.total_angles - ch * kAC);
         if (!clamp)
-            sample_chunk<false, true>(S, buf, count, ch * kAC, P, fX, nfY, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<false, true>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         else if (fast)
-            sample_chunk<true, true>(S, buf, count, ch * kAC, P, fX, nfY, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, true>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         else
-            sample_chunk<true, false>(S, buf, count, ch * kAC, P, fX, nfY, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, false>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         __syncthreads();
     }
     if (P.n_subsets > 0) {
