@@ -448,18 +448,19 @@ def serve_section(ufoir, ctx):
     return out
 
 
-# the other configured workloads: (name, method, n_dets, n_angles, phantom side, phantom kind, I0, params)
+# the other configured workloads:
+# (name, method, n_dets, n_angles, phantom side, phantom kind, I0, slices, params)
 METHOD_CASES = (
-    ("C1 SART 367^2 x 180 angles, 10 iterations", "sart", 367, 180, 256, "ellipses", None,
+    ("C1 SART 367^2 x 180 angles, 10 iterations", "sart", 367, 180, 256, "ellipses", None, 1,
      dict(num_iterations=10)),
-    ("C2 SIRT one slice 1448^2 x 1200 angles, 10 iterations", "sirt", 1448, 1200, 1024, "ellipses", 1e5,
+    ("C2 SIRT one slice 1448^2 x 1200 angles, 10 iterations", "sirt", 1448, 1200, 1024, "ellipses", 1e5, 1,
      dict(num_iterations=10)),
     ("C3a ASD-POCS 2900^2 x 90 angles, 1 outer iteration (inner SART 10)", "asdpocs", 2900, 90, 2048, "polygons",
-     1e4, dict(num_iterations=1)),
+     1e4, 1, dict(num_iterations=1)),
     ("C3b ASD-POCS 2900^2 x 360 angles, 1 outer iteration (inner SART 10)", "asdpocs", 2900, 360, 2048,
-     "polygons", 1e4, dict(num_iterations=1)),
-    ("C4 SBTV 1448^2 x 720 angles, 1 outer iteration", "sbtv", 1448, 720, 1024, "ellipses", 1e5,
-     {"num_iterations": 1, "lambda": 0.05, "mu": 1.0}),
+     "polygons", 1e4, 1, dict(num_iterations=1)),
+    ("C4 SBTV 1448^2 x 720 angles, 16 slices (one batch of the 512), 1 outer iteration", "sbtv", 1448, 720, 1024,
+     "ellipses", 1e5, 16, {"num_iterations": 1, "lambda": 0.05, "mu": 1.0}),
 )
 
 
@@ -468,16 +469,17 @@ def methods_section(ufoir, ctx):
     resident in HBM: the call time (after one untimed call) and its rate."""
     from ufoir import synth
     out = []
-    for name, method, n, na, P, kind, i0, kw in METHOD_CASES:
+    for name, method, n, na, P, kind, i0, S, kw in METHOD_CASES:
         step = float(np.float32(np.pi / na))
-        vol = synth.phantom_for(n, P, kind, seed=7000 + n + na)
+        vols = np.stack([synth.phantom_for(n, P, kind, seed=7000 + n + na + i) for i in range(S)])
         proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=1)
-        sino = proj.forward(vol, np.zeros((na, n), np.float32))
+        sino = proj.forward(vols, np.zeros((S, na, n), np.float32))
         proj.close()
         if i0:
-            sino, _ = synth.poisson_noise(sino, i0, seed=8000 + n + na)
+            for i in range(S):
+                sino[i], _ = synth.poisson_noise(sino[i], i0, seed=8000 + n + na + i)
         d_sino = ufoir.DeviceArray.from_numpy(ctx, sino.astype(np.float32))
-        d_vol = ufoir.DeviceArray(ctx, (n, n), zero=True)
+        d_vol = ufoir.DeviceArray(ctx, (S, n, n), zero=True)
         proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=0)
         fn = getattr(ufoir, method)
         fn(proj, d_sino, d_vol, **kw)
@@ -486,8 +488,8 @@ def methods_section(ufoir, ctx):
         fn(proj, d_sino, d_vol, **kw)
         ms = ctx.timer_end()
         iters = kw["num_iterations"]
-        out.append({"workload": name, "ms_per_call": ms, "ms_per_iteration": ms / iters,
-                    "samples_per_iteration_fp_bp": 2.0 * n * n * na})
+        out.append({"workload": name, "slices": S, "ms_per_call": ms, "ms_per_iteration": ms / iters,
+                    "ms_per_slice_iteration": ms / iters / S, "samples_per_slice_iteration_fp_bp": 2.0 * n * n * na})
         proj.close()
         d_sino.close()
         d_vol.close()

@@ -125,6 +125,25 @@ def test_sbtv_matches_oracle(ufoir_lib, gpu_ctx, oracle, mode):
     assert err64 < 0.1
 
 
+def test_sbtv_batched_slices_match_single_slice_runs(ufoir_lib, gpu_ctx, oracle):
+    # 18 slices run as a batch of 16 and a batch of 2; the slices differ in
+    # scale and content, so their CGS runs take different branches and exits,
+    # and each must equal the oracle's run of that slice alone
+    n, na = 24, 20
+    rng = np.random.default_rng(44)
+    step = np.float32(np.pi / na)
+    op = oracle.projector(n, na, step)
+    sinos = np.stack([oracle.forward(op, (rng.random((n, n), dtype=np.float32) ** (1 + i % 4)) * (1 + 3 * i))
+                      for i in range(18)])
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    got = ufoir_lib.sbtv(p, sinos, num_iterations=2, norm_mode=ufoir_lib.NORM_COMPAT, mu=1.0,
+                         **{"lambda": 0.05})
+    prm = oracle.sbtv_params(num_iterations=2, lambda_=0.05, mu=1.0, norm_mode=oracle.NORM_COMPAT)
+    for i in range(18):
+        want, _ = oracle.sbtv(op, sinos[i], prm)
+        assert np.array_equal(got[i], want), (i, float(np.abs(got[i] - want).max()))
+
+
 def test_norms_match_oracle(ufoir_lib, gpu_ctx, oracle):
     rng = np.random.default_rng(5)
     for h, w in [(1, 1), (7, 13), (64, 64), (300, 257)]:

@@ -757,199 +757,291 @@ done:
 /* ------------------------------------------------------------------------ */
 /* Split-Bregman TV                                                         */
 /* ------------------------------------------------------------------------ */
+/*
+ * SBTV runs S slices in lockstep: processA, the difference operators and the
+ * inner products work on all S slices in one launch each, while every
+ * slice keeps its own CGS scalars, branches and exits (sbtv-task.c:404-585)
+ * on the host, exactly as the per-slice algorithm. A slice that leaves the
+ * CGS loop is no longer updated; processA still computes it (its result is
+ * discarded), so each slice sees the same operations in the same order as
+ * when it runs alone.
+ */
+#define SBTV_MAX_BATCH 16
+
 typedef struct {
     ufoir_projector *p;
     udev *d;
     udev_geom g;
     size_t n, nv, ns;
+    int S;
     float lambda, mu;
     int mode;
     float *tmpA, *tmpAt, *tmpD, *tmpDxt;
     ufoir_fp_scratch fs;
 } sbtv_ctx;
 
-/* processA (sbtv-task.c:587-635): out = mu A^T A in + lambda (Dxt Dx in + Dyt Dy in). */
+/* processA (sbtv-task.c:587-635): out = mu A^T A in + lambda (Dxt Dx in + Dyt Dy in), S slices. */
 static int sbtv_processA(sbtv_ctx *c, const float *in, float *out)
 {
     udev *d = c->d;
-    const int n = (int) c->n;
-    int rc = udev_fill(d, c->tmpA, c->ns, 0.0f);
+    const int n = (int) c->n, S = c->S;
+    const size_t nvS = c->nv * (size_t) S;
+    int rc = udev_fill(d, c->tmpA, c->ns * (size_t) S, 0.0f);
     if (!rc)
-        rc = ufoir__fp_full(c->p, &c->fs, in, c->tmpA, NULL, 0, c->tmpA, c->p->prm.correction_scale, 1);
+        rc = ufoir__fp_full(c->p, &c->fs, in, c->tmpA, NULL, 0, c->tmpA, c->p->prm.correction_scale, S);
     if (!rc)
         rc = udev_bp(d, &c->g, c->p->subsets, (int) c->p->n_subsets, c->tmpA, NULL, NULL, 0, NULL, c->tmpAt,
-                     c->p->prm.relaxation, 1);
+                     c->p->prm.relaxation, S);
     if (!rc)
-        rc = udev_unary(d, UDEV_SCALE, c->tmpAt, c->mu, 0, c->tmpAt, c->nv);
+        rc = udev_unary(d, UDEV_SCALE, c->tmpAt, c->mu, 0, c->tmpAt, nvS);
     if (!rc)
-        rc = udev_diff(d, UDEV_DY, in, c->tmpD, n, n, 1);
+        rc = udev_diff(d, UDEV_DY, in, c->tmpD, n, n, S);
     if (!rc)
-        rc = udev_diff(d, UDEV_DYT, c->tmpD, out, n, n, 1);
+        rc = udev_diff(d, UDEV_DYT, c->tmpD, out, n, n, S);
     if (!rc)
-        rc = udev_diff(d, UDEV_DX, in, c->tmpD, n, n, 1);
+        rc = udev_diff(d, UDEV_DX, in, c->tmpD, n, n, S);
     if (!rc)
-        rc = udev_diff(d, UDEV_DXT, c->tmpD, c->tmpDxt, n, n, 1);
+        rc = udev_diff(d, UDEV_DXT, c->tmpD, c->tmpDxt, n, n, S);
     if (!rc)
-        rc = udev_binary(d, UDEV_ADD, out, c->tmpDxt, 0, out, c->nv);
+        rc = udev_binary(d, UDEV_ADD, out, c->tmpDxt, 0, out, nvS);
     if (!rc)
-        rc = udev_unary(d, UDEV_SCALE, out, c->lambda, 0, out, c->nv);
+        rc = udev_unary(d, UDEV_SCALE, out, c->lambda, 0, out, nvS);
     if (!rc)
-        rc = udev_binary(d, UDEV_ADD, out, c->tmpAt, 0, out, c->nv);
+        rc = udev_binary(d, UDEV_ADD, out, c->tmpAt, 0, out, nvS);
     return rc;
 }
 
-static int sbtv_dot(sbtv_ctx *c, const float *a, const float *b, float *out)
+/* the reference's inner product of every slice (one launch, one read-back) */
+static int sbtv_dots(sbtv_ctx *c, const float *a, const float *b, float *out)
 {
-    return udev_dot(c->d, a, b, c->n, c->n, 1, c->mode, out);
+    return udev_dot(c->d, a, b, c->n, c->n, c->S, c->mode, out);
 }
 
 /* l2_norm (basic-ops-processor.c:239-247): sqrt in double of the float dot. */
-static int sbtv_l2(sbtv_ctx *c, const float *a, float *out)
+static int sbtv_l2s(sbtv_ctx *c, const float *a, float *out)
 {
-    float dotv = 0;
-    int rc = sbtv_dot(c, a, a, &dotv);
-    if (!rc)
-        *out = (float) sqrt((double) dotv);
+    int rc = sbtv_dots(c, a, a, out);
+    for (int s = 0; s < c->S && !rc; s++)
+        out[s] = (float) sqrt((double) out[s]);
     return rc;
 }
 
-static int copy_d(sbtv_ctx *c, float *dst, const float *src)
+#define SL(ptr, s) ((ptr) + (size_t) (s) * c->nv)
+
+static int copy_s(sbtv_ctx *c, float *dst, const float *src, int s)
 {
-    return udev_memcpy_async(c->d, dst, src, c->nv * sizeof(float));
+    return udev_memcpy_async(c->d, SL(dst, s), SL(src, s), c->nv * sizeof(float));
 }
 
-/* cgs (sbtv-task.c:404-585). */
+static int op_s(sbtv_ctx *c, int op, const float *a, const float *b, float m, float *out, int s)
+{
+    return udev_binary(c->d, op, SL(a, s), SL(b, s), m, SL(out, s), c->nv);
+}
+
+/* per-slice CGS state */
+typedef struct {
+    float n2b, tolb, normr, normr_act, normmin, rho, alpha;
+    unsigned int flag, stag, moresteps;
+    int active;      /* still iterating */
+    int finished;    /* left before the loop ("initial guess is good enough") */
+} cgs_slice;
+
+/* cgs (sbtv-task.c:404-585) on S slices. */
 static int sbtv_cgs(sbtv_ctx *c, const float *b, float *x, const float *x0, unsigned int max_iter, float **w)
 {
     udev *d = c->d;
-    const size_t nv = c->nv;
+    const int S = c->S;
+    const size_t nvS = c->nv * (size_t) S;
     float *xmin = w[0], *r = w[1], *rt = w[2], *u = w[3], *tmpa = w[4], *pp = w[5], *ph = w[6], *q = w[7];
     float *vh = w[8], *tempSum = w[9], *uh = w[10], *qh = w[11];
     int rc;
     const float tol = 1E-06f;
-    float n2b;
-    if ((rc = sbtv_l2(c, b, &n2b)))
-        return rc;
-    if ((rc = copy_d(c, x, x0)))
-        return rc;
-    unsigned int flag = 1;
-    if ((rc = copy_d(c, xmin, x)))
-        return rc;
-    const float tolb = tol * n2b;
-    if ((rc = sbtv_processA(c, x, r)))
-        return rc;
-    if ((rc = udev_binary(d, UDEV_SUB, b, r, 0, r, nv)))
-        return rc;
-    float normr, normr_act;
-    if ((rc = sbtv_l2(c, r, &normr)))
-        return rc;
-    normr_act = normr;
-    if (normr <= tolb)
-        return UFOIR_OK;   /* "Initial guess is good enough" (:434-440) */
-    if ((rc = copy_d(c, rt, r)))
-        return rc;
-    float normmin = normr;
-    float rho = 1.0f;
-    unsigned int stag = 0, moresteps = 0;
     const unsigned int maxmsteps = 5, maxstagsteps = 3;
-    if ((rc = udev_fill(d, u, nv, 0.0f)) || (rc = udev_fill(d, tmpa, nv, 0.0f)) ||
-        (rc = udev_fill(d, pp, nv, 0.0f)) || (rc = udev_fill(d, q, nv, 0.0f)) ||
-        (rc = udev_fill(d, tempSum, nv, 0.0f)))
+    cgs_slice st[SBTV_MAX_BATCH];
+    float v[SBTV_MAX_BATCH], v2[SBTV_MAX_BATCH];
+    memset(st, 0, sizeof(st));
+    if ((rc = sbtv_l2s(c, b, v)))
+        return rc;
+    if ((rc = udev_memcpy_async(d, x, x0, nvS * sizeof(float))) ||
+        (rc = udev_memcpy_async(d, xmin, x, nvS * sizeof(float))))
+        return rc;
+    for (int s = 0; s < S; s++) {
+        st[s].n2b = v[s];
+        st[s].flag = 1;
+        st[s].tolb = tol * st[s].n2b;
+    }
+    if ((rc = sbtv_processA(c, x, r)) || (rc = udev_binary(d, UDEV_SUB, b, r, 0, r, nvS)) ||
+        (rc = sbtv_l2s(c, r, v)))
+        return rc;
+    int n_active = 0;
+    for (int s = 0; s < S; s++) {
+        st[s].normr = st[s].normr_act = v[s];
+        if (st[s].normr <= st[s].tolb) {
+            st[s].finished = 1;   /* "Initial guess is good enough" (:434-440) */
+            continue;
+        }
+        st[s].active = 1;
+        st[s].normmin = st[s].normr;
+        st[s].rho = 1.0f;
+        n_active++;
+        if ((rc = copy_s(c, rt, r, s)))
+            return rc;
+    }
+    if ((rc = udev_fill(d, u, nvS, 0.0f)) || (rc = udev_fill(d, tmpa, nvS, 0.0f)) ||
+        (rc = udev_fill(d, pp, nvS, 0.0f)) || (rc = udev_fill(d, q, nvS, 0.0f)) ||
+        (rc = udev_fill(d, tempSum, nvS, 0.0f)))
         return rc;
 
-    for (unsigned int iter = 0; iter < max_iter; ++iter) {
-        const float rho1 = rho;
-        if ((rc = sbtv_dot(c, rt, r, &rho)))
+    for (unsigned int iter = 0; iter < max_iter && n_active > 0; ++iter) {
+        float rho1[SBTV_MAX_BATCH];
+        if ((rc = sbtv_dots(c, rt, r, v)))
             return rc;
-        if (rho == 0 || isinf(rho) || isnan(rho)) {
-            flag = 4;
-            break;
-        }
-        if (iter == 0) {
-            if ((rc = copy_d(c, u, r)) || (rc = copy_d(c, pp, u)))
-                return rc;
-        } else {
-            const float beta = rho / rho1;
-            if (beta == 0 || isinf(beta) || isnan(beta)) {
-                flag = 4;
-                break;
+        for (int s = 0; s < S; s++) {
+            if (!st[s].active)
+                continue;
+            rho1[s] = st[s].rho;
+            st[s].rho = v[s];
+            const float rho = st[s].rho;
+            if (rho == 0 || isinf(rho) || isnan(rho)) {
+                st[s].flag = 4;
+                st[s].active = 0;
+                continue;
             }
-            if ((rc = udev_binary(d, UDEV_ADD_SCALED, r, q, beta, u, nv)) ||
-                (rc = udev_binary(d, UDEV_ADD_SCALED, q, pp, beta, tempSum, nv)) ||
-                (rc = udev_binary(d, UDEV_ADD_SCALED, u, tempSum, beta, pp, nv)))
-                return rc;
-        }
-        if ((rc = copy_d(c, ph, pp)) || (rc = sbtv_processA(c, ph, vh)))
-            return rc;
-        float rtvh;
-        if ((rc = sbtv_dot(c, rt, vh, &rtvh)))
-            return rc;
-        float alpha = 0;
-        if (rtvh == 0) {
-            flag = 4;
-            break;
-        } else {
-            alpha = rho / rtvh;
-        }
-        if (isinf(alpha) || isnan(alpha)) {
-            flag = 4;
-            break;
-        }
-        if ((rc = udev_binary(d, UDEV_ADD_SCALED, u, vh, -alpha, q, nv)) ||
-            (rc = udev_binary(d, UDEV_ADD, u, q, 0, uh, nv)))
-            return rc;
-        float l2uh, l2x;
-        if ((rc = sbtv_l2(c, uh, &l2uh)) || (rc = sbtv_l2(c, x, &l2x)))
-            return rc;
-        /* fabs() promotes to double; EPS is the double literal 2.2204E-16 (:35, :498) */
-        if (fabs((double) alpha) * (double) l2uh < 2.2204E-16 * (double) l2x)
-            stag += 1;
-        else
-            stag = 0;
-        if ((rc = udev_binary(d, UDEV_ADD_SCALED, x, uh, alpha, x, nv)) || (rc = sbtv_processA(c, uh, qh)) ||
-            (rc = udev_binary(d, UDEV_ADD_SCALED, r, qh, -alpha, r, nv)))
-            return rc;
-        if ((rc = sbtv_l2(c, r, &normr)))
-            return rc;
-        normr_act = normr;
-        if (normr <= tolb || stag >= maxstagsteps || moresteps) {
-            /* the reference applies A to r here (:535) */
-            if ((rc = sbtv_processA(c, r, tmpa)) || (rc = udev_binary(d, UDEV_SUB, b, tmpa, 0, r, nv)) ||
-                (rc = sbtv_l2(c, r, &normr_act)))
-                return rc;
-            if (normr_act <= tolb) {
-                flag = 0;
-                break;
+            if (iter == 0) {
+                if ((rc = copy_s(c, u, r, s)) || (rc = copy_s(c, pp, u, s)))
+                    return rc;
             } else {
-                if (stag >= maxstagsteps && moresteps == 0)
-                    stag = 0;
-                moresteps += 1;
-                if (moresteps >= maxmsteps) {
-                    flag = 3;
-                    break;
+                const float beta = rho / rho1[s];
+                if (beta == 0 || isinf(beta) || isnan(beta)) {
+                    st[s].flag = 4;
+                    st[s].active = 0;
+                    continue;
+                }
+                if ((rc = op_s(c, UDEV_ADD_SCALED, r, q, beta, u, s)) ||
+                    (rc = op_s(c, UDEV_ADD_SCALED, q, pp, beta, tempSum, s)) ||
+                    (rc = op_s(c, UDEV_ADD_SCALED, u, tempSum, beta, pp, s)))
+                    return rc;
+            }
+            if ((rc = copy_s(c, ph, pp, s)))
+                return rc;
+        }
+        if ((rc = sbtv_processA(c, ph, vh)) || (rc = sbtv_dots(c, rt, vh, v)))
+            return rc;
+        for (int s = 0; s < S; s++) {
+            if (!st[s].active)
+                continue;
+            if (v[s] == 0) {
+                st[s].flag = 4;
+                st[s].active = 0;
+                continue;
+            }
+            st[s].alpha = st[s].rho / v[s];
+            if (isinf(st[s].alpha) || isnan(st[s].alpha)) {
+                st[s].flag = 4;
+                st[s].active = 0;
+                continue;
+            }
+            if ((rc = op_s(c, UDEV_ADD_SCALED, u, vh, -st[s].alpha, q, s)) || (rc = op_s(c, UDEV_ADD, u, q, 0, uh, s)))
+                return rc;
+        }
+        if ((rc = sbtv_l2s(c, uh, v)) || (rc = sbtv_l2s(c, x, v2)))
+            return rc;
+        for (int s = 0; s < S; s++) {
+            if (!st[s].active)
+                continue;
+            /* fabs() promotes to double; EPS is the double literal 2.2204E-16 (:35, :498) */
+            if (fabs((double) st[s].alpha) * (double) v[s] < 2.2204E-16 * (double) v2[s])
+                st[s].stag += 1;
+            else
+                st[s].stag = 0;
+            if ((rc = op_s(c, UDEV_ADD_SCALED, x, uh, st[s].alpha, x, s)))
+                return rc;
+        }
+        if ((rc = sbtv_processA(c, uh, qh)))
+            return rc;
+        for (int s = 0; s < S; s++)
+            if (st[s].active && (rc = op_s(c, UDEV_ADD_SCALED, r, qh, -st[s].alpha, r, s)))
+                return rc;
+        if ((rc = sbtv_l2s(c, r, v)))
+            return rc;
+        int check = 0;
+        for (int s = 0; s < S; s++) {
+            if (!st[s].active)
+                continue;
+            st[s].normr = st[s].normr_act = v[s];
+            if (st[s].normr <= st[s].tolb || st[s].stag >= maxstagsteps || st[s].moresteps)
+                check = 1;
+        }
+        if (check) {
+            /* the reference applies A to r here (:535) */
+            if ((rc = sbtv_processA(c, r, tmpa)))
+                return rc;
+            int any = 0;
+            for (int s = 0; s < S; s++) {
+                if (!st[s].active ||
+                    !(st[s].normr <= st[s].tolb || st[s].stag >= maxstagsteps || st[s].moresteps))
+                    continue;
+                if ((rc = op_s(c, UDEV_SUB, b, tmpa, 0, r, s)))
+                    return rc;
+                any = 1;
+            }
+            if (any && (rc = sbtv_l2s(c, r, v)))
+                return rc;
+            for (int s = 0; s < S; s++) {
+                if (!st[s].active ||
+                    !(st[s].normr <= st[s].tolb || st[s].stag >= maxstagsteps || st[s].moresteps))
+                    continue;
+                st[s].normr_act = v[s];
+                if (st[s].normr_act <= st[s].tolb) {
+                    st[s].flag = 0;
+                    st[s].active = 0;
+                } else {
+                    if (st[s].stag >= maxstagsteps && st[s].moresteps == 0)
+                        st[s].stag = 0;
+                    st[s].moresteps += 1;
+                    if (st[s].moresteps >= maxmsteps) {
+                        st[s].flag = 3;
+                        st[s].active = 0;
+                    }
                 }
             }
         }
-        if (normr_act < normmin) {
-            normmin = normr_act;
-            if ((rc = copy_d(c, xmin, x)))
-                return rc;
-        }
-        if (stag >= maxstagsteps) {
-            flag = 3;
-            break;
+        n_active = 0;
+        for (int s = 0; s < S; s++) {
+            if (!st[s].active)
+                continue;
+            if (st[s].normr_act < st[s].normmin) {
+                st[s].normmin = st[s].normr_act;
+                if ((rc = copy_s(c, xmin, x, s)))
+                    return rc;
+            }
+            if (st[s].stag >= maxstagsteps) {
+                st[s].flag = 3;
+                st[s].active = 0;
+                continue;
+            }
+            n_active++;
         }
     }
-    if (flag != 0) {
-        float l2r;
-        if ((rc = sbtv_processA(c, xmin, tmpa)) || (rc = udev_binary(d, UDEV_SUB, b, tmpa, 0, r, nv)) ||
-            (rc = sbtv_l2(c, r, &l2r)))
+    int any_flag = 0;
+    for (int s = 0; s < S; s++)
+        any_flag |= !st[s].finished && st[s].flag != 0;
+    if (any_flag) {
+        if ((rc = sbtv_processA(c, xmin, tmpa)))
             return rc;
-        if (l2r <= normr_act && (rc = copy_d(c, x, xmin)))
+        for (int s = 0; s < S; s++)
+            if (!st[s].finished && st[s].flag != 0 && (rc = op_s(c, UDEV_SUB, b, tmpa, 0, r, s)))
+                return rc;
+        if ((rc = sbtv_l2s(c, r, v)))
             return rc;
+        for (int s = 0; s < S; s++)
+            if (!st[s].finished && st[s].flag != 0 && v[s] <= st[s].normr_act && (rc = copy_s(c, x, xmin, s)))
+                return rc;
     }
     return UFOIR_OK;
 }
+
+#undef SL
 
 /* normalization (basic-ops-processor.c:342-367), in place on the device. */
 static int sbtv_normalize(udev *d, float *v, size_t count)
@@ -979,6 +1071,7 @@ int ufoir_sbtv_process(ufoir_projector *proj, const ufoir_sbtv_params *prm, cons
     if (rc)
         return rc;
     const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
+    const int S_max = n_slices < SBTV_MAX_BATCH ? (int) n_slices : SBTV_MAX_BATCH;
     udev *d = ctx->dev;
     sbtv_ctx c;
     memset(&c, 0, sizeof(c));
@@ -997,66 +1090,71 @@ int ufoir_sbtv_process(ufoir_projector *proj, const ufoir_sbtv_params *prm, cons
     float *f = NULL;
     UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bo, vol, nv * n_slices, 0));
-    UFOIR_TRY(ufoir__alloc(ctx, &f, ns));
-    UFOIR_TRY(ufoir__alloc(ctx, &c.tmpA, ns));
+    UFOIR_TRY(ufoir__alloc(ctx, &f, ns * (size_t) S_max));
+    UFOIR_TRY(ufoir__alloc(ctx, &c.tmpA, ns * (size_t) S_max));
     for (int i = 0; i < SBTV_NBUF; i++)
-        UFOIR_TRY(ufoir__alloc(ctx, &buf[i], nv));
+        UFOIR_TRY(ufoir__alloc(ctx, &buf[i], nv * (size_t) S_max));
     c.tmpAt = buf[12];
     c.tmpD = buf[13];
     c.tmpDxt = buf[14];
-    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &c.fs, 1));
+    UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &c.fs, (size_t) S_max));
     float *fbp = buf[16], *up = buf[17], *bvec = buf[18], *bx = buf[19], *by = buf[20], *dx = buf[21];
     float *dy = buf[22], *tmpx = buf[23], *tmpy = buf[24], *tmp = buf[25];
 
-    for (size_t s = 0; s < n_slices; s++) {
-        float *u = bo.dev + s * nv;
+    for (size_t s0 = 0; s0 < n_slices; s0 += (size_t) S_max) {
+        const int S = n_slices - s0 < (size_t) S_max ? (int) (n_slices - s0) : S_max;
+        const size_t nvS = nv * (size_t) S;
+        c.S = S;
+        float *u = bo.dev + s0 * nv;
         /* normalise the input (a copy; the reference does it in place, :239),
-         * copy it to f and normalise f again (:246-248) */
-        UFOIR_TRY(udev_memcpy_async(d, f, bb.dev + s * ns, ns * sizeof(float)));
-        UFOIR_TRY(sbtv_normalize(d, f, ns));
-        UFOIR_TRY(sbtv_normalize(d, f, ns));
+         * copy it to f and normalise f again (:246-248), per slice */
+        UFOIR_TRY(udev_memcpy_async(d, f, bb.dev + s0 * ns, ns * (size_t) S * sizeof(float)));
+        for (int s = 0; s < S; s++) {
+            UFOIR_TRY(sbtv_normalize(d, f + (size_t) s * ns, ns));
+            UFOIR_TRY(sbtv_normalize(d, f + (size_t) s * ns, ns));
+        }
         /* fbp = A^T f (:251-253), u = 0, bx = by = dx = dy = 0, fbp *= mu (:279) */
         UFOIR_TRY(udev_bp(d, &c.g, proj->subsets, (int) proj->n_subsets, f, NULL, NULL, 0, NULL, fbp,
-                          proj->prm.relaxation, 1));
-        UFOIR_TRY(udev_fill(d, u, nv, 0.0f));
-        UFOIR_TRY(udev_fill(d, bx, nv, 0.0f));
-        UFOIR_TRY(udev_fill(d, by, nv, 0.0f));
-        UFOIR_TRY(udev_fill(d, dx, nv, 0.0f));
-        UFOIR_TRY(udev_fill(d, dy, nv, 0.0f));
-        UFOIR_TRY(udev_unary(d, UDEV_SCALE, fbp, c.mu, 0, fbp, nv));
+                          proj->prm.relaxation, S));
+        UFOIR_TRY(udev_fill(d, u, nvS, 0.0f));
+        UFOIR_TRY(udev_fill(d, bx, nvS, 0.0f));
+        UFOIR_TRY(udev_fill(d, by, nvS, 0.0f));
+        UFOIR_TRY(udev_fill(d, dx, nvS, 0.0f));
+        UFOIR_TRY(udev_fill(d, dy, nvS, 0.0f));
+        UFOIR_TRY(udev_unary(d, UDEV_SCALE, fbp, c.mu, 0, fbp, nvS));
         const float d_lambda = (float) -1 / c.lambda;
 
         for (unsigned int it = 0; it < prm->num_iterations; ++it) {
-            UFOIR_TRY(udev_memcpy_async(d, up, u, nv * sizeof(float)));
+            UFOIR_TRY(udev_memcpy_async(d, up, u, nvS * sizeof(float)));
             /* calculate_b (:304-334) */
-            UFOIR_TRY(udev_binary(d, UDEV_SUB, dx, bx, 0, tmp, nv));
-            UFOIR_TRY(udev_diff(d, UDEV_DXT, tmp, tmpx, (int) n, (int) n, 1));
-            UFOIR_TRY(udev_binary(d, UDEV_SUB, dy, by, 0, tmp, nv));
-            UFOIR_TRY(udev_diff(d, UDEV_DYT, tmp, tmpy, (int) n, (int) n, 1));
-            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpx, tmpy, 0, bvec, nv));
-            UFOIR_TRY(udev_unary(d, UDEV_SCALE, bvec, c.lambda, 0, bvec, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_ADD, fbp, bvec, 0, bvec, nv));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, dx, bx, 0, tmp, nvS));
+            UFOIR_TRY(udev_diff(d, UDEV_DXT, tmp, tmpx, (int) n, (int) n, S));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, dy, by, 0, tmp, nvS));
+            UFOIR_TRY(udev_diff(d, UDEV_DYT, tmp, tmpy, (int) n, (int) n, S));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpx, tmpy, 0, bvec, nvS));
+            UFOIR_TRY(udev_unary(d, UDEV_SCALE, bvec, c.lambda, 0, bvec, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, fbp, bvec, 0, bvec, nvS));
 
             UFOIR_TRY(sbtv_cgs(&c, bvec, u, up, 30, buf));
 
             /* update_db (:336-402) */
             float *s_ = buf[0], *top = buf[1], *e12 = buf[2];
-            UFOIR_TRY(udev_diff(d, UDEV_DX, u, tmpx, (int) n, (int) n, 1));
-            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpx, bx, 0, tmpx, nv));
-            UFOIR_TRY(udev_diff(d, UDEV_DY, u, tmpy, (int) n, (int) n, 1));
-            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpy, by, 0, tmpy, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmpx, tmpx, 0, s_, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmpy, tmpy, 0, tmp, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_ADD, s_, tmp, 0, s_, nv));
-            UFOIR_TRY(udev_unary(d, UDEV_SQRT, s_, 0, 0, s_, nv));
-            UFOIR_TRY(udev_unary(d, UDEV_ADDC, s_, d_lambda, 0, top, nv));
-            UFOIR_TRY(udev_unary(d, UDEV_MAXC, top, 0.0f, 0, top, nv));
-            UFOIR_TRY(udev_unary(d, UDEV_MAXC, s_, 1E-12f, 0, e12, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_DIV, top, e12, 0, tmp, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmp, tmpx, 0, dx, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmp, tmpy, 0, dy, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_SUB, tmpx, dx, 0, bx, nv));
-            UFOIR_TRY(udev_binary(d, UDEV_SUB, tmpy, dy, 0, by, nv));
+            UFOIR_TRY(udev_diff(d, UDEV_DX, u, tmpx, (int) n, (int) n, S));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpx, bx, 0, tmpx, nvS));
+            UFOIR_TRY(udev_diff(d, UDEV_DY, u, tmpy, (int) n, (int) n, S));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, tmpy, by, 0, tmpy, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmpx, tmpx, 0, s_, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmpy, tmpy, 0, tmp, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_ADD, s_, tmp, 0, s_, nvS));
+            UFOIR_TRY(udev_unary(d, UDEV_SQRT, s_, 0, 0, s_, nvS));
+            UFOIR_TRY(udev_unary(d, UDEV_ADDC, s_, d_lambda, 0, top, nvS));
+            UFOIR_TRY(udev_unary(d, UDEV_MAXC, top, 0.0f, 0, top, nvS));
+            UFOIR_TRY(udev_unary(d, UDEV_MAXC, s_, 1E-12f, 0, e12, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_DIV, top, e12, 0, tmp, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmp, tmpx, 0, dx, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_MUL, tmp, tmpy, 0, dy, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, tmpx, dx, 0, bx, nvS));
+            UFOIR_TRY(udev_binary(d, UDEV_SUB, tmpy, dy, 0, by, nvS));
         }
     }
     UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
@@ -1068,7 +1166,7 @@ done:
     ufoir__fp_scratch_free(proj, &c.fs);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bo);
-    udev_sync(d);
+    udev_sync(ctx->dev);
     return rc;
 }
 
