@@ -184,3 +184,28 @@ def test_method_argument_errors(ufoir_lib, gpu_ctx):
         ufoir_lib.asdpocs(q, sino, ng=5000)
     out = ufoir_lib.sirt(q, sino, num_iterations=1)
     assert np.isfinite(out).all()
+
+
+def test_c2_full_size_batched_sirt_iteration_matches_oracle(ufoir_lib, gpu_ctx, oracle):
+    # The headline configuration (1448 bins, 1200 angles, 1024^2 ellipse
+    # phantom) through the batched, graph-captured path that bench.py times:
+    # one SIRT iteration, bit for bit against the oracle (about 1e10 oracle
+    # samples, OpenMP over the host cores).
+    from ufoir import synth
+    n, na = 1448, 1200
+    step = np.float32(np.pi / na)
+    oracle.set_threads(os.cpu_count() or 1)
+    op = oracle.projector(n, na, step)
+    sino = oracle.forward(op, synth.ellipse_phantom(n, 1024, 10, seed=2000))
+    want = oracle.sirt(op, sino, 1, 0.25)
+    p = ufoir_lib.ParallelProjector(gpu_ctx, step=float(step), angles_num=na, is_forward=0)
+    d_sino = ufoir_lib.DeviceArray.from_numpy(gpu_ctx, sino[None])
+    d_vol = ufoir_lib.DeviceArray(gpu_ctx, (1, n, n), zero=True)
+    batch = ufoir_lib.SirtBatch(p, d_sino, d_vol, relaxation_factor=0.25)
+    batch.run(1)
+    got = d_vol.download()[0]
+    batch.close()
+    assert rel_l2(got, want) <= TOL_ITER and np.array_equal(got, want)
+    d_sino.close()
+    d_vol.close()
+    p.close()

@@ -111,18 +111,6 @@ __device__ __forceinline__ float lds(uint32_t addr)
 constexpr float kFloorMagic = 12582912.0f;
 constexpr int kFloorMagicBits = 0x4B400000;
 
-/* One exact linear-filter tap pair read from shared memory: row_base is the
- * 32-bit shared address of element 0 of the row, minus 4 * kFloorMagicBits. */
-__device__ __forceinline__ float sample_smem(float c, uint32_t row_base)
-{
-    const float cm = __fsub_rn(c, 0.5f);
-    const float y = __fadd_rd(cm, kFloorMagic);
-    const float fi = __fsub_rn(y, kFloorMagic);
-    const float t = __fsub_rn(cm, fi);
-    const uint32_t addr = row_base + 4u * (uint32_t) __float_as_int(y);
-    return lerp(t, lds(addr), lds(addr + 4u));
-}
-
 /*
  * Paired forms for two samples at once, on the packed FP32 instructions of
  * sm_100 and later (PTX add/sub/mul/fma .f32x2). Each lane rounds exactly as
@@ -171,14 +159,6 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b)
 {
     unsigned long long r;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
-    return unpack2(r);
-}
-
-/* a * b, for products that are not added afterwards */
-__device__ __forceinline__ float2 mul2(float2 a, float2 b)
-{
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
     return unpack2(r);
 }
 
