@@ -40,10 +40,10 @@ N_DETS, N_ANGLES, PHANTOM, SLICES, I0, RELAX = 1448, 1200, 1024, 64, 1e5, 0.25
 E2E_ITERS = 10
 CPU_SAMPLE_ANGLES = 300
 # serve trace: the configured request mix, scaled to seconds of GPU time
-SERVE_JOBS = 16
+SERVE_JOBS = 48
 SERVE_RATE = 200.0
 SERVE_SIZES = ((256, 367), (512, 724), (1024, 1448), (2048, 2900))
-SERVE_ITER_SCALE = 100
+SERVE_ITER_SCALE = 25
 SERVE_BUDGET = 150 * 10**9
 SERVE_SEED = 5005
 
@@ -464,6 +464,31 @@ METHOD_CASES = (
 )
 
 
+# methods whose whole call the oracle port runs in seconds on the host cores
+METHOD_CPU = ("sart", "asdpocs")
+
+
+def method_cpu_baseline(method, n, na, step, sino, kw):
+    """The oracle port (the reference's kernels and host loop restated in C,
+    OpenMP over the NDRange) on the first slice of a method workload, the same
+    call as the GPU's, on all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    p = pyoracle.projector(n, na, step)
+    sino = np.ascontiguousarray(sino, np.float32)
+    t0 = time.perf_counter()
+    if method == "sart":
+        pyoracle.sart(p, sino, kw["num_iterations"], 0.25)
+    else:
+        pyoracle.asdpocs(p, sino, pyoracle.asdpocs_params(num_iterations=kw["num_iterations"],
+                                                         norm_mode=pyoracle.NORM_FP64))
+    dt = time.perf_counter() - t0
+    return {"ms_per_call": dt * 1e3, "cores": threads, "kind": "port", "sample": "the whole call, slice 0"}
+
+
 def methods_section(ufoir, ctx):
     """One call of each other configured method workload on one slice,
     resident in HBM: the call time (after one untimed call) and its rate."""
@@ -488,8 +513,11 @@ def methods_section(ufoir, ctx):
         fn(proj, d_sino, d_vol, **kw)
         ms = ctx.timer_end()
         iters = kw["num_iterations"]
-        out.append({"workload": name, "slices": S, "ms_per_call": ms, "ms_per_iteration": ms / iters,
-                    "ms_per_slice_iteration": ms / iters / S, "samples_per_slice_iteration_fp_bp": 2.0 * n * n * na})
+        row = {"workload": name, "slices": S, "ms_per_call": ms, "ms_per_iteration": ms / iters,
+               "ms_per_slice_iteration": ms / iters / S, "samples_per_slice_iteration_fp_bp": 2.0 * n * n * na}
+        if method in METHOD_CPU:
+            row["cpu_baseline"] = method_cpu_baseline(method, n, na, np.float32(step), sino[0], kw)
+        out.append(row)
         proj.close()
         d_sino.close()
         d_vol.close()
