@@ -76,8 +76,17 @@ UFOIR_API void ufoir_ctx_destroy(ufoir_ctx *ctx);
 /* Message of the last failed call on this context ("" if none). */
 UFOIR_API const char *ufoir_last_error(const ufoir_ctx *ctx);
 UFOIR_API int ufoir_ctx_synchronize(ufoir_ctx *ctx);
-/* The context's cudaStream_t, as an opaque pointer. */
+/* The stream the context's work is queued on (a cudaStream_t, opaque). */
 UFOIR_API void *ufoir_ctx_stream(ufoir_ctx *ctx);
+/* Queue the context's work on the caller's stream from now on (NULL: back
+ * to the context's own stream), so that the library's kernels are ordered
+ * with the caller's own work without host synchronisation. The stream must
+ * belong to the context's device and must not be capturing a graph while a
+ * method runs (SIRT and SART capture their iterations themselves). Calls
+ * that return host results still wait for this stream. Stands in for the
+ * per-call stream argument of a stream-based interface; the reference has
+ * one in-order OpenCL queue per node (src/tasks/ufo-ir-sart-task.c:162). */
+UFOIR_API int ufoir_ctx_set_stream(ufoir_ctx *ctx, void *stream);
 /* Device memory helpers (stream-ordered on the context's stream). */
 UFOIR_API int ufoir_device_alloc(ufoir_ctx *ctx, size_t bytes, void **ptr);
 UFOIR_API int ufoir_device_free(ufoir_ctx *ctx, void *ptr);

@@ -220,6 +220,36 @@ def test_fp_with_few_tiles_splits_detectors(ufoir_lib, gpu_ctx, oracle, n, na, a
         assert rel_l2(got[i], want) <= TOL_ONE and np.array_equal(got[i], want)
 
 
+def test_work_queued_on_a_callers_stream(ufoir_lib, gpu_ctx, oracle):
+    # another context's stream stands in for a stream the caller owns
+    other = ufoir_lib.Context(0)
+    s = other.stream()
+    n, na = 64, 90
+    step = np.float32(np.pi / na)
+    vol = np.random.default_rng(9).random((n, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step)
+    want = oracle.forward(oracle.projector(n, na, step), vol)
+    gpu_ctx.set_stream(s)
+    try:
+        assert gpu_ctx.stream() == s
+        got = p.forward(vol, np.zeros((na, n), np.float32))      # host buffers: staged and waited for
+        d_vol = ufoir_lib.DeviceArray.from_numpy(gpu_ctx, vol)
+        d_sino = ufoir_lib.DeviceArray(gpu_ctx, (na, n), zero=True)
+        p.forward(d_vol, d_sino)
+        other.synchronize()                                       # the caller orders on its own stream
+        got2 = d_sino.download()
+        p.set(is_forward=0)
+        rec = ufoir_lib.sirt(p, want, num_iterations=2)           # captured iterations on the caller's stream
+        d_vol.close()
+        d_sino.close()
+    finally:
+        gpu_ctx.set_stream(None)
+    assert gpu_ctx.stream() != s
+    assert np.array_equal(got, want) and np.array_equal(got2, want)
+    assert np.array_equal(rec, oracle.sirt(oracle.projector(n, na, step), want, 2, 0.25))
+    other.close()
+
+
 def test_errors_are_reported_not_fatal(ufoir_lib, gpu_ctx):
     with pytest.raises(ufoir_lib.UfoirError) as e:
         ufoir_lib.ParallelProjector(gpu_ctx, model="siddon")

@@ -74,6 +74,14 @@ void *ufoir_ctx_stream(ufoir_ctx *ctx)
     return ctx ? udev_stream(ctx->dev) : NULL;
 }
 
+int ufoir_ctx_set_stream(ufoir_ctx *ctx, void *stream)
+{
+    if (!ctx)
+        return UFOIR_ERR_INVALID;
+    udev_use_stream(ctx->dev, stream);
+    return UFOIR_OK;
+}
+
 uint64_t ufoir_ctx_kernel_launches(const ufoir_ctx *ctx)
 {
     return ctx ? udev_launches(ctx->dev) : 0;

@@ -118,7 +118,7 @@ _lib = None
 # Every symbol include/ufoir.h declares (checked by the CPU test suite).
 EXPORTED = (
     "ufoir_ctx_create", "ufoir_ctx_destroy", "ufoir_last_error", "ufoir_ctx_synchronize",
-    "ufoir_ctx_stream", "ufoir_device_alloc", "ufoir_device_free", "ufoir_host_alloc",
+    "ufoir_ctx_stream", "ufoir_ctx_set_stream", "ufoir_device_alloc", "ufoir_device_free", "ufoir_host_alloc",
     "ufoir_host_free", "ufoir_memcpy", "ufoir_ctx_kernel_launches",
     "ufoir_projector_params_init", "ufoir_projector_create", "ufoir_projector_destroy",
     "ufoir_projector_get_params", "ufoir_projector_set_params", "ufoir_projector_get_requisition",
@@ -161,6 +161,7 @@ def _declare(L):
     L.ufoir_ctx_synchronize.argtypes = [vp]
     L.ufoir_ctx_stream.argtypes = [vp]
     L.ufoir_ctx_stream.restype = vp
+    L.ufoir_ctx_set_stream.argtypes = [vp, vp]
     L.ufoir_device_alloc.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
     L.ufoir_device_free.argtypes = [vp, vp]
     L.ufoir_host_alloc.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
@@ -323,6 +324,10 @@ class Context:
         ms = C.c_float()
         self._check(lib().ufoir_ctx_timer_end(self.handle, C.byref(ms)))
         return ms.value
+
+    def set_stream(self, stream):
+        """Queue this context's work on `stream` (a cudaStream_t as int; None: its own stream)."""
+        self._check(lib().ufoir_ctx_set_stream(self.handle, stream))
 
     def sample_ceiling(self) -> float:
         """Interpolated samples/s of the forward projector's per-sample sequence, no global traffic."""
