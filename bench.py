@@ -298,8 +298,9 @@ def run_ufoir(args, dist):
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "traffic": traffic * S if traffic else None,
                 "algorithmic_bytes_per_launch": dom_bytes,
-                "note": "compulsory bytes / kernel time; the projectors are bound by interpolated-sample "
-                        "issue, not HBM, so this fraction is small by construction"}
+                "note": "compulsory bytes / kernel time against the measured HBM copy rate; the projectors "
+                        "are bound by the FMA pipe (packed FP32 interpolation), not HBM, so this fraction is "
+                        "small by construction; compute_bound gives the kernel against its measured ceiling"}
     ceiling = ctx.sample_ceiling()
     fp_rate = fp_samples / (kernel_ms["fp"] / 1e3)
     bp_rate = bp_samples / (kernel_ms["bp"] / 1e3)
@@ -310,6 +311,12 @@ def run_ufoir(args, dist):
                    "bp_frac": bp_rate / ceiling if ceiling else None,
                    "ceiling": "measured in this run (ufoir_sample_ceiling): the FP's exact per-sample "
                               "sequence from shared memory on every SM, no global traffic"}
+    dom_rate = fp_rate if dom == "fp" else bp_rate
+    roofline["compute_bound"] = {
+        "kernel": roofline["kernel"], "achieved": dom_rate, "peak": ceiling, "unit": "samples/s",
+        "frac": dom_rate / ceiling if ceiling else None,
+        "peak_source": "measured in this run: ufoir_sample_ceiling (the FP's per-sample packed-FP32 "
+                       "sequence from shared memory on every SM)"}
 
     out = {"metric": METRIC, "value": value, "unit": "slice-iters/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
