@@ -59,6 +59,49 @@ def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, sli
         assert np.array_equal(got[i], want), (i, np.abs(got[i] - want).max())
 
 
+# Sizes above 512 detectors split a ray's 64-sample blocks over several CTAs
+# of the per-angle forward projection (the last CTA adds the block sums);
+# off-centre axes give inactive detectors and clamped backprojection tiles.
+@pytest.mark.parametrize("n,na,axis,iters,slices", [(513, 24, -1.0, 1, 1), (600, 40, 290.6, 2, 2),
+                                                     (1111, 30, -1.0, 1, 1), (1448, 36, 700.25, 1, 1),
+                                                     (2900, 12, -1.0, 1, 1)])
+def test_sart_chunked_sizes_match_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
+    rng = np.random.default_rng(5 * n + na)
+    step = np.float32(np.pi / na)
+    sinos = rng.random((slices, na, n), dtype=np.float32) * n
+    p = _method_proj(ufoir_lib, gpu_ctx, step, axis)
+    got = ufoir_lib.sart(p, sinos, num_iterations=iters, relaxation_factor=0.3)
+    for i in range(slices):
+        want = oracle.sart(oracle.projector(n, na, step, axis), sinos[i], iters, 0.3)
+        assert np.array_equal(got[i], want), (i, np.abs(got[i] - want).max())
+
+
+# An axis within half a pixel of the image edge crosses the backprojection's
+# clamp edges; SART then runs the general per-angle kernels.
+@pytest.mark.parametrize("axis", [0.25, 23.8])
+def test_sart_crossed_clamp_edges_match_oracle(ufoir_lib, gpu_ctx, oracle, axis):
+    n, na = 24, 20
+    step = np.float32(np.pi / na)
+    sino = np.random.default_rng(77).random((na, n), dtype=np.float32) * n
+    p = _method_proj(ufoir_lib, gpu_ctx, step, axis)
+    got = ufoir_lib.sart(p, sino, num_iterations=2, relaxation_factor=0.25)
+    want = oracle.sart(oracle.projector(n, na, step, axis), sino, 2, 0.25)
+    assert np.array_equal(got, want), np.abs(got - want).max()
+
+
+def test_asdpocs_chunked_size_matches_oracle(ufoir_lib, gpu_ctx, oracle):
+    n, na = 530, 24
+    step = np.float32(np.pi / na)
+    vol = np.random.default_rng(23).random((n, n), dtype=np.float32)
+    sino = oracle.forward(oracle.projector(n, na, step), vol)
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    got = ufoir_lib.asdpocs(p, sino, num_iterations=2, norm_mode=ufoir_lib.NORM_COMPAT,
+                            df_minimizer=dict(num_iterations=2, relaxation_factor=0.25))
+    prm = oracle.asdpocs_params(num_iterations=2, sart_iterations=2, norm_mode=oracle.NORM_COMPAT)
+    want, _ = oracle.asdpocs(oracle.projector(n, na, step), sino, prm)
+    assert np.array_equal(got, want), np.abs(got - want).max()
+
+
 def test_methods_golden_fixture_compat(ufoir_lib, gpu_ctx):
     d = np.load(os.path.join(GOLDEN, "methods_n20_a18.npz"))
     step = np.float32(d["step"])

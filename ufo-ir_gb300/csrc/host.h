@@ -68,9 +68,10 @@ typedef struct {
 } ufoir__sirt_iter;
 int ufoir__sirt_body(void *arg);
 
-/* One SART sweep (every angle in order) over n_slices slices. xT holds the
- * volume transposed during the horizontal direction run; table holds the
- * block-start coordinates of the per-angle forward projection. */
+/* One SART sweep (every angle in order) over n_slices slices. work holds the
+ * padded copies of the volume in the layouts of the two direction runs (or,
+ * for crossed clamp edges, its transpose); table holds the block-start
+ * coordinates of the per-angle forward projection. */
 typedef struct {
     ufoir_projector *p;
     udev_geom g;
@@ -79,12 +80,12 @@ typedef struct {
     const float *R;
     float lambda;
     int n_slices;
-    float *xT, *table;
+    float *work, *table;
     const float *relax_dev;     /* if not NULL, lambda is read from here */
 } ufoir__sart_iter;
 int ufoir__sart_body(void *arg);
-/* The sweep's scratch (xT, table; the geometry must be prepared). */
-int ufoir__sart_scratch_alloc(ufoir_projector *p, float **xT, float **table, int n_slices);
+/* The sweep's scratch (work, zero-filled, and table; the geometry must be prepared). */
+int ufoir__sart_scratch_alloc(ufoir_projector *p, float **work, float **table, int n_slices);
 size_t ufoir__sart_scratch_bytes(size_t n, size_t na, size_t n_slices);
 
 /* ASD-POCS split into setup, one outer iteration and release, so that the
@@ -98,7 +99,7 @@ typedef struct {
     const float *b;
     float *out;
     float *x, *x_prev, *x_res, *b_res, *grad, *R;
-    float *xT, *table;                  /* SART sweep scratch */
+    float *work, *table;                /* SART sweep scratch */
     ufoir_fp_scratch fs;
     float *scal;                        /* device scalar block (dsc points into it) */
     double *partials;                   /* FP64 norm partials of this state */

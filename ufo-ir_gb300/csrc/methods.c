@@ -379,17 +379,41 @@ int ufoir__sart_body(void *arg)
     const int n = s->g.n_dets, S = s->n_slices;
     int rc = UFOIR_OK;
     /* sart-task.c:209-217: per angle, r_theta = (b_theta - A_theta x) * R_theta;
-     * x = x + lambda A_theta^T r_theta. The volume is held transposed while
-     * the angles are horizontal, so that every ray walks rows. */
+     * x = x + lambda A_theta^T r_theta. The volume lives in the layout of the
+     * current direction run, transposed while the angles are horizontal, so
+     * that every ray walks rows. */
+    if (udev_sart_padded(&s->g)) {
+        /* padded copies V (vertical run) and H (horizontal run) in s->work */
+        int place = -1;
+        for (unsigned int a = 0; a < s->p->n_angles && rc == UFOIR_OK; a++) {
+            const int dir = s->p->h_dir[a];
+            const int want = dir == UFOIR_HORIZONTAL;
+            if (want != place) {
+                rc = udev_sart_move(d, n, s->x, s->work, place, want, S);
+                place = want;
+            }
+            if (!rc)
+                rc = udev_sart_fp(d, &s->g, (int) a, dir, s->table, s->work, place, s->b, s->R, 1, s->resid, -1.0f,
+                                  S);
+            if (!rc)
+                rc = udev_sart_bp(d, &s->g, (int) a, s->p->h_sin[a], s->p->h_cos[a], s->resid, s->work, place,
+                                  s->lambda, s->relax_dev, S);
+        }
+        if (!rc && place >= 0)
+            rc = udev_sart_move(d, n, s->x, s->work, place, -1, S);
+        return rc;
+    }
+    /* crossed clamp edges (axis within half a pixel of the image edge): the
+     * general kernels on the unpadded volume and its transpose in s->work */
     int transposed = 0;
     for (unsigned int a = 0; a < s->p->n_angles && rc == UFOIR_OK; a++) {
         const int dir = s->p->h_dir[a];
         const int want = dir == UFOIR_HORIZONTAL;
         if (want != transposed) {
-            rc = udev_transpose(d, transposed ? s->xT : s->x, transposed ? s->x : s->xT, n, S);
+            rc = udev_transpose(d, transposed ? s->work : s->x, transposed ? s->x : s->work, n, S);
             transposed = want;
         }
-        float *vol = transposed ? s->xT : s->x;
+        float *vol = transposed ? s->work : s->x;
         if (!rc)
             rc = udev_fp_angle(d, &s->g, (int) a, dir, s->table, vol, s->b, s->R, 1, s->resid, -1.0f, S);
         if (!rc)
@@ -397,22 +421,25 @@ int ufoir__sart_body(void *arg)
                                s->lambda, s->relax_dev, S);
     }
     if (!rc && transposed)
-        rc = udev_transpose(d, s->xT, s->x, n, S);
+        rc = udev_transpose(d, s->work, s->x, n, S);
     return rc;
 }
 
 size_t ufoir__sart_scratch_bytes(size_t n, size_t na, size_t n_slices)
 {
-    return sizeof(float) * (n * n * n_slices + udev_fp_block_starts_floats((int) n, (int) na));
+    return sizeof(float) * (udev_sart_work_floats((int) n, (int) n_slices) + udev_fp_block_starts_floats((int) n, (int) na));
 }
 
-int ufoir__sart_scratch_alloc(ufoir_projector *p, float **xT, float **table, int n_slices)
+int ufoir__sart_scratch_alloc(ufoir_projector *p, float **work, float **table, int n_slices)
 {
     ufoir_ctx *ctx = p->ctx;
     const size_t n = p->n_dets;
+    const size_t wf = udev_sart_work_floats((int) n, n_slices);
     udev_geom g;
     ufoir__projector_geom(p, &g);
-    int rc = ufoir__alloc(ctx, xT, n * n * (size_t) n_slices);
+    int rc = ufoir__alloc(ctx, work, wf);
+    if (!rc)
+        rc = udev_memset(ctx->dev, *work, 0, sizeof(float) * wf);   /* the pads stay zero */
     if (!rc)
         rc = ufoir__alloc(ctx, table, udev_fp_block_starts_floats((int) n, (int) p->n_angles));
     if (!rc)
@@ -422,7 +449,7 @@ int ufoir__sart_scratch_alloc(ufoir_projector *p, float **xT, float **table, int
 
 /* One SART call on resident buffers: x = SART(b), R precomputed. */
 static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, const float *b, float *x,
-                    float *resid, const float *R, float *xT, float *table, int n_slices)
+                    float *resid, const float *R, float *work, float *table, int n_slices)
 {
     ufoir_ctx *ctx = proj->ctx;
     const size_t n = proj->n_dets, nv = n * n;
@@ -440,7 +467,7 @@ static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, con
     it.R = R;
     it.lambda = lambda;
     it.n_slices = n_slices;
-    it.xT = xT;
+    it.work = work;
     it.table = table;
     it.relax_dev = NULL;
     /* one angle sweep per graph: a sweep is already 2 * n_angles kernels */
@@ -459,7 +486,7 @@ static int sart_run(ufoir_projector *proj, unsigned int iters, float lambda, con
     for (unsigned int i = 0; i < iters && rc == UFOIR_OK; i++)
         rc = udev_graph_launch(ctx->dev, exec, kernels);
     if (rc == UFOIR_OK)
-        rc = udev_sync(ctx->dev);
+        rc = udev_take_kernel_error(ctx->dev);   /* waits for the stream */
     udev_graph_destroy(exec);
     return rc;
 }
@@ -478,21 +505,21 @@ int ufoir_sart_process(ufoir_projector *proj, const ufoir_sart_params *prm, cons
         return rc;
     const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
     ufoir_buf bb = {0}, bx = {0};
-    float *R = NULL, *resid = NULL, *xT = NULL, *table = NULL;
+    float *R = NULL, *resid = NULL, *work = NULL, *table = NULL;
     UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
     UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices > nv ? ns * n_slices : nv));
-    UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &xT, &table, (int) n_slices));
+    UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &work, &table, (int) n_slices));
     proj->prm.correction_scale = 1.0f;
     UFOIR_TRY(ufoir__ray_weights(proj, R, resid));
-    UFOIR_TRY(sart_run(proj, prm->num_iterations, prm->relaxation_factor, bb.dev, bx.dev, resid, R, xT, table,
+    UFOIR_TRY(sart_run(proj, prm->num_iterations, prm->relaxation_factor, bb.dev, bx.dev, resid, R, work, table,
                        (int) n_slices));
     UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
 done:
     ufoir__free(ctx, R);
     ufoir__free(ctx, resid);
-    ufoir__free(ctx, xT);
+    ufoir__free(ctx, work);
     ufoir__free(ctx, table);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bx);
@@ -533,12 +560,12 @@ void ufoir__asd_release(ufoir__asd_state *s)
     ufoir__free(ctx, s->b_res);
     ufoir__free(ctx, s->grad);
     ufoir__free(ctx, s->R);
-    ufoir__free(ctx, s->xT);
+    ufoir__free(ctx, s->work);
     ufoir__free(ctx, s->table);
     ufoir__free(ctx, s->scal);
     ufoir__free(ctx, s->partials);
     ufoir__fp_scratch_free(s->p, &s->fs);
-    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = s->xT = s->table = s->scal = NULL;
+    s->x = s->x_prev = s->x_res = s->b_res = s->grad = s->R = s->work = s->table = s->scal = NULL;
     s->partials = NULL;
 }
 
@@ -640,7 +667,7 @@ int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asd
     UFOIR_TRY(ufoir__alloc(ctx, &s->R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &s->scal, asd_scalar_floats((size_t) S)));
     UFOIR_TRY(udev_malloc(ctx->dev, (void **) &s->partials, sizeof(double) * (udev_l1_partials(S) + 1)));
-    UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &s->xT, &s->table, S));
+    UFOIR_TRY(ufoir__sart_scratch_alloc(proj, &s->work, &s->table, S));
     UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &s->fs, (size_t) S));
     s->dsc.beta = s->scal;
     s->dsc.relax = s->scal + 1;
@@ -682,7 +709,7 @@ int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asd
     s->sweep.lambda = 0.0f;
     s->sweep.relax_dev = s->dsc.relax;
     s->sweep.n_slices = S;
-    s->sweep.xT = s->xT;
+    s->sweep.work = s->work;
     s->sweep.table = s->table;
     UFOIR_TRY(capture(ctx->dev, ufoir__sart_body, &s->sweep, &s->sart_exec, &s->sart_kernels));
     UFOIR_TRY(capture(ctx->dev, asd_post_body, s, &s->post_exec, &s->post_kernels));
@@ -745,6 +772,7 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
     UFOIR_TRY(ufoir__asd_setup(&st, proj, prm, bb.dev, bo.dev, (int) n_slices));
     for (unsigned int it = 0; it < prm->num_iterations; it++)
         UFOIR_TRY(ufoir__asd_outer(&st));
+    UFOIR_TRY(udev_take_kernel_error(ctx->dev));
     UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
 done:
     ufoir__asd_release(&st);

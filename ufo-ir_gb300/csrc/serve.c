@@ -40,7 +40,7 @@ typedef struct job {
     int busy;
     void *stream, *event;
     ufoir_projector *proj;
-    float *b, *x, *R, *C, *resid, *xT, *table;
+    float *b, *x, *R, *C, *resid, *work, *table;
     ufoir__sirt_iter sirt;
     ufoir__sart_iter sart;
     ufoir__asd_state asd;
@@ -170,11 +170,11 @@ static void job_release(ufoir_server *s, job *j)
     ufoir__free(ctx, j->R);
     ufoir__free(ctx, j->C);
     ufoir__free(ctx, j->resid);
-    ufoir__free(ctx, j->xT);
+    ufoir__free(ctx, j->work);
     ufoir__free(ctx, j->table);
     if (j->sirt.fs.P || j->sirt.fs.TP)
         ufoir__fp_scratch_free(j->proj, &j->sirt.fs);
-    j->b = j->x = j->R = j->C = j->resid = j->xT = j->table = NULL;
+    j->b = j->x = j->R = j->C = j->resid = j->work = j->table = NULL;
     if (j->stream)
         udev_sync(ctx->dev);
     udev_use_stream(ctx->dev, NULL);
@@ -260,7 +260,7 @@ static int job_start(ufoir_server *s, job *j)
         break;
     case UFOIR_METHOD_SART:
         if ((rc = ufoir__alloc(ctx, &j->R, ns)) || (rc = ufoir__alloc(ctx, &j->resid, ns > nv ? ns : nv)) ||
-            (rc = ufoir__sart_scratch_alloc(p, &j->xT, &j->table, 1)))
+            (rc = ufoir__sart_scratch_alloc(p, &j->work, &j->table, 1)))
             return rc;
         p->prm.correction_scale = 1.0f;
         if ((rc = ufoir__ray_weights(p, j->R, j->resid)))
@@ -277,7 +277,7 @@ static int job_start(ufoir_server *s, job *j)
         j->sart.R = j->R;
         j->sart.lambda = jd->sart.relaxation_factor;
         j->sart.n_slices = 1;
-        j->sart.xT = j->xT;
+        j->sart.work = j->work;
         j->sart.table = j->table;
         if ((rc = capture_body(s, j, ufoir__sart_body, &j->sart)))
             return rc;

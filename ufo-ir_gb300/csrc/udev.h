@@ -86,6 +86,21 @@ int udev_fp_angle(udev *d, const udev_geom *g, int angle, int dir, const float *
  * with the value it points to when the kernel runs. */
 int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino, float *vol,
                   int transposed, float relax, const float *relax_dev, int n_slices);
+/* The padded sweep layout: two zero-padded copies of the volume, V (rows =
+ * image rows) and H (the transpose), whole 64-row blocks high. The work
+ * area (udev_sart_work_floats floats) must be zero-filled once. */
+int udev_sart_pitch(int n);
+size_t udev_sart_work_floats(int n, int n_slices);
+/* 1 if the padded kernels serve this geometry (clamp edges e0 <= e1). */
+int udev_sart_padded(const udev_geom *g);
+/* Copies the volume between the user's slices (place -1), V (0) and H (1). */
+int udev_sart_move(udev *d, int n, float *x, float *work, int from, int to, int n_slices);
+/* udev_fp_angle and udev_bp_angle on the padded copy `place` (0 V for
+ * vertical rays, 1 H for horizontal ones). */
+int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, const float *table, float *work, int place,
+                 const float *src, const float *w, int w_shared, float *out, float scale, int n_slices);
+int udev_sart_bp(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino, float *work,
+                 int place, float relax, const float *relax_dev, int n_slices);
 
 /* ---- Tiled forward projector (all angles, shared-memory row streaming) ---- */
 /* Row pitch (floats, multiple of 4) of the padded images: 2 zero columns,

@@ -304,9 +304,13 @@ int udev_take_kernel_error(udev *d)
         return UFOIR_OK;
     UDEV_CHECK(d, cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream));
     UDEV_CHECK(d, cudaStreamSynchronize(d->stream));
-    udev_set_error(d, "a kernel gave up waiting for a shared-memory copy (code %d); results of that call are invalid",
-                   code);
-    return UFOIR_ERR_TIMEOUT;
+    if (code & 3) {
+        udev_set_error(d, "a kernel gave up waiting for a shared-memory copy (code %d); results of that call are invalid",
+                       code);
+        return UFOIR_ERR_TIMEOUT;
+    }
+    udev_set_error(d, "a kernel found its staging buffer too small (code %d); results of that call are invalid", code);
+    return UFOIR_ERR_CUDA;
 }
 
 int udev_timer_begin(udev *d)

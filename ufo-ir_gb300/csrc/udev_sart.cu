@@ -4,20 +4,27 @@
  * angle's backprojection, n_angles times per sweep (sart-task.c:209-217).
  *
  * One angle is only n rays of n samples, so a ray-per-thread kernel leaves
- * the GPU idle. Here a ray is cut into its 64-sample blocks (the blocks the
- * reference sums separately, projector-parallel-joseph.cl:81-93) and every
- * (ray, block) pair is a thread. The coordinate at each block start is the
+ * the GPU idle. A ray is cut into its 64-sample blocks (the blocks the
+ * reference sums separately, projector-parallel-joseph.cl:81-93), and the
+ * blocks are computed in parallel. The coordinate at each block start is the
  * float recurrence c += step replayed from the ray start; it depends only on
- * the geometry, so it is tabulated once per job (block_starts_kernel) and a
- * block's thread starts from the table with the exact value the sequential
- * walk reaches. The block sums of a ray are then added in order in shared
- * memory, exactly as the reference adds its inner sums.
+ * the geometry, so it is tabulated once per job (block_starts_kernel), and a
+ * block starts from the table with the exact value the sequential walk
+ * reaches. The block sums of a ray are then added in order, exactly as the
+ * reference adds its inner sums.
  *
  * Rays walk rows of a row-major image: vertical rays the volume, horizontal
  * rays its transpose. SART keeps the volume in the layout of the current
- * direction run (the angles of [0, pi) form three runs) and transposes it
- * at the two run boundaries; the per-angle backprojection updates either
- * layout in place.
+ * direction run (the angles of [0, pi) form three runs) and transposes it at
+ * the two run boundaries; the per-angle backprojection updates either layout
+ * in place. Two sets of kernels:
+ *  - the padded path (sart_fp_kernel, sart_bp_kernel, sart_copy_kernel):
+ *    zero-padded copies of the volume, a cluster of CTAs per group of 64
+ *    rays whose block sums meet in distributed shared memory, and a tiled
+ *    backprojection with the tile's sinogram span in shared memory;
+ *  - the general kernels (fp_angle_kernel, bp_angle_kernel) on the
+ *    unpadded volume, for geometries whose backprojection clamp edges cross
+ *    (an axis within half a pixel of the image edge).
  */
 #include <cuda_runtime.h>
 
@@ -229,6 +236,403 @@ __global__ void __launch_bounds__(256) bp_angle_kernel(BpAngleArgs P)
     }
 }
 
+/*
+ * The padded sweep layout. While a sweep runs, the volume lives in one of
+ * two padded copies: V (row y holds the pixels of row y) for vertical
+ * angles, H (row x holds column x, the transpose) for horizontal ones. A
+ * padded row has kSartPadL zero columns, the n pixels (16-byte aligned),
+ * and at least 3 zero columns; the rows run up to whole 64-row blocks, the
+ * rows beyond n zero. Forward-projection rays then read their taps without
+ * bounds checks: the coordinate is clamped to [-1, n + 1], where both taps
+ * outside the image are pad zeros, as the reference's zero border gives, and
+ * samples in rows >= n read zero rows (…joseph.cl:81-93 sums fixed
+ * 64-sample blocks). The backprojection updates only the pixels, so the
+ * pads stay zero.
+ */
+constexpr int kSartPadL = 4;
+constexpr int kErrSpan = 4;      /* error word: a backprojection span exceeded its buffer */
+
+__host__ __device__ inline int sart_pitch(int n)
+{
+    return (n + kSartPadL + 3 + 3) / 4 * 4;
+}
+
+__host__ __device__ inline int sart_rows(int n)
+{
+    return (n + kBlock - 1) / kBlock * kBlock;
+}
+
+/* dst = src (or its transpose) for n x n interiors, each addressed by a row
+ * pitch and a column offset. Grid (ceil(n/32), ceil(n/32), slices), block 32 x 8. */
+__global__ void __launch_bounds__(256) sart_copy_kernel(const float *__restrict__ src, int sp, int so,
+                                                        long long sstride, float *__restrict__ dst, int dp, int dof,
+                                                        long long dstride, int n, int transpose)
+{
+    __shared__ float tile[32][33];
+    const int bx = (int) blockIdx.x * 32, by = (int) blockIdx.y * 32;
+    const int tx = (int) threadIdx.x;
+    src += (size_t) blockIdx.z * sstride;
+    dst += (size_t) blockIdx.z * dstride;
+    if (!transpose) {
+        for (int k = (int) threadIdx.y; k < 32; k += 8) {
+            const int y = by + k, x = bx + tx;
+            if (x < n && y < n)
+                dst[(size_t) y * dp + dof + x] = src[(size_t) y * sp + so + x];
+        }
+        return;
+    }
+    for (int k = (int) threadIdx.y; k < 32; k += 8) {
+        const int y = by + k, x = bx + tx;
+        tile[k][tx] = (x < n && y < n) ? src[(size_t) y * sp + so + x] : 0.0f;
+    }
+    __syncthreads();
+    for (int k = (int) threadIdx.y; k < 32; k += 8) {
+        const int y = bx + k, x = by + tx;   /* dst(y, x) = src(x, y) */
+        if (x < n && y < n)
+            dst[(size_t) y * dp + dof + x] = tile[tx][k];
+    }
+}
+
+struct SartFpArgs {
+    const float *img;          /* padded layout walked by this angle's rays, [slices][rows][pitch] */
+    const float *table;        /* [n_angles][n_blocks][n] block-start coordinates */
+    const float *src;
+    const float *w;
+    float *out;
+    const float *sinv;
+    const float *cosv;
+    int n;
+    int n_blocks;
+    int angle;
+    int dir;
+    int pitch;
+    int cluster;               /* CTAs per ray group (the cluster size) */
+    float axis;
+    float scale;
+    float neg_zero;
+    long long img_stride;
+    long long sino_stride;
+    long long w_stride;
+};
+
+constexpr int kFpCluster = 8;                       /* CTAs per ray group at most (portable cluster) */
+constexpr int kFpLocal = kMaxBlocks / kFpCluster;   /* blocks per CTA at most */
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+/* A float of CTA `rank`'s shared memory, at the address `local` has here. */
+__device__ __forceinline__ float ld_cluster(const float *local, int rank)
+{
+    uint32_t remote;
+    float v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(remote)
+                 : "r"((uint32_t) __cvta_generic_to_shared(local)), "r"(rank));
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(remote) : "memory");
+    return v;
+}
+
+/* The samples [row0, row0 + rows) of rays (s0, s1) of one block, from the
+ * coordinates c at row0: appends them to the running sum (Q == 1) or
+ * stores them in v (Q > 1). All loads of 16 samples are in flight together. */
+template <int ROWS, bool STREAM>
+__device__ __forceinline__ void sart_fp_samples(const float *img, int pitch, float2 c, float2 st, float hi,
+                                                float2 z2, float2 &run, float2 *v)
+{
+    constexpr int K = 16;
+#pragma unroll 1
+    for (int k0 = 0; k0 < ROWS; k0 += K) {
+        float2 t[K];
+        int ia[K], ib[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float2 cc = make_float2(fminf(fmaxf(c.x, -1.0f), hi), fminf(fmaxf(c.y, -1.0f), hi));
+            const float2 y = joseph::floor_any2(cc, t[k]);
+            const int roff = (k0 + k) * pitch;
+            ia[k] = __float_as_int(y.x) + roff;
+            ib[k] = __float_as_int(y.y) + roff;
+            c = joseph::add2(c, st);
+        }
+        float2 t0[K], t1[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            t0[k] = make_float2(__ldg(img + ia[k]), __ldg(img + ib[k]));
+            t1[k] = make_float2(__ldg(img + ia[k] + 1), __ldg(img + ib[k] + 1));
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (STREAM)
+                run = joseph::add2(run, joseph::lerp2(t[k], t0[k], t1[k], z2));
+            else
+                v[k] = joseph::lerp2(t[k], t0[k], t1[k], z2);
+        }
+    }
+}
+
+/*
+ * out = (src + scale * S) [* w] for the rays of one angle, on the padded layout.
+ *
+ * Lane l walks rays 64g + l and 64g + l + 32 together in packed FP32, so
+ * every load instruction of a warp reads 32 adjacent rays' taps in one
+ * image row. A ray's block starts at its table coordinate and advances by
+ * the float recurrence c += step; each block's inner sum adds its 64
+ * samples in order (…joseph.cl:84-92).
+ *
+ * The blocks of one group of 64 rays are spread over a cluster of C CTAs
+ * (block b on CTA b mod C), each keeping its block sums in shared memory.
+ * SEG == 4: the CTA's four warps cut each of its blocks into four 16-row
+ * segments, computed with all loads in flight together, and fold the inner
+ * sum through the segments in order (warp q continues the running sum of
+ * warp q - 1), for few blocks per CTA. SEG == 1: each warp adds whole
+ * blocks, for many. After a cluster barrier, CTA 0 reads the block sums
+ * over distributed shared memory, adds them in block order and writes the
+ * rays' results (…joseph.cl:93-100); a second barrier keeps every CTA's
+ * shared memory alive until then. Grid (groups * C, 1, slices), cluster
+ * (C, 1, 1), 128 threads.
+ */
+template <int SEG>
+__global__ void __launch_bounds__(128, 3) sart_fp_kernel(SartFpArgs P)
+{
+    __shared__ float bs_local[kFpLocal][64];
+    __shared__ float2 run_s[32];
+    const int lane = (int) (threadIdx.x & 31);
+    const int warp = (int) (threadIdx.x >> 5);
+    const int C = P.cluster;
+    const int g = (int) blockIdx.x / C, rank = (int) blockIdx.x % C;
+    const int slice = (int) blockIdx.z;
+    const int n = P.n, nb = P.n_blocks;
+    const int s0 = g * 64 + lane, s1 = s0 + 32;
+
+    /* CTA 0 fetches its rays' src and w early */
+    const int sr = g * 64 + (int) threadIdx.x;
+    const bool writer = rank == 0 && threadIdx.x < 64 && sr < n;
+    const size_t oidx = (size_t) slice * P.sino_stride + (size_t) P.angle * n + sr;
+    float src_v = 0.0f, w_v = 0.0f;
+    if (writer) {
+        src_v = P.src[oidx];
+        if (P.w)
+            w_v = P.w[(size_t) slice * P.w_stride + (size_t) P.angle * n + sr];
+    }
+
+    float det_step, step;
+    joseph::ray_steps(P.dir, __ldg(P.sinv + P.angle), __ldg(P.cosv + P.angle), det_step, step);
+    const float2 st = joseph::splat(step), z2 = joseph::splat(P.neg_zero);
+    const float hi = (float) (n + 1);
+    const float *tab = P.table + (size_t) P.angle * nb * n;
+    const float *img0 = P.img + (size_t) slice * P.img_stride + kSartPadL - joseph::kFloorMagicBits;
+
+    if (SEG == 4) {
+        for (int i = 0; rank + C * i < nb; ++i) {
+            const int b = rank + C * i;
+            const float *tb = tab + (size_t) b * n;
+            float2 c = make_float2(__ldg(tb + min(s0, n - 1)), __ldg(tb + min(s1, n - 1)));
+            for (int k = 0; k < 16 * warp; ++k)
+                c = joseph::add2(c, st);
+            float2 v[16], run = joseph::splat(0.0f);
+            sart_fp_samples<16, false>(img0 + (size_t) (b * kBlock + 16 * warp) * P.pitch, P.pitch, c, st, hi, z2,
+                                       run, v);
+            /* inner = (((0 + v_0) + v_1) + ... + v_63), segment by segment */
+#pragma unroll
+            for (int stage = 0; stage < 4; ++stage) {
+                if (warp == stage) {
+                    if (stage > 0)
+                        run = run_s[lane];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k)
+                        run = joseph::add2(run, v[k]);
+                    if (stage < 3)
+                        run_s[lane] = run;
+                }
+                __syncthreads();
+            }
+            if (warp == 3) {
+                bs_local[i][lane] = run.x;
+                bs_local[i][lane + 32] = run.y;
+            }
+        }
+    } else {
+        for (int i = warp; rank + C * i < nb; i += 4) {
+            const int b = rank + C * i;
+            const float *tb = tab + (size_t) b * n;
+            const float2 c = make_float2(__ldg(tb + min(s0, n - 1)), __ldg(tb + min(s1, n - 1)));
+            float2 run = joseph::splat(0.0f);
+            sart_fp_samples<kBlock, true>(img0 + (size_t) b * kBlock * P.pitch, P.pitch, c, st, hi, z2, run,
+                                          nullptr);
+            bs_local[i][lane] = run.x;
+            bs_local[i][lane + 32] = run.y;
+        }
+    }
+    cluster_sync_all();
+    if (writer) {
+        float result = src_v;
+        const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
+        if (!joseph::detector_inactive(kc, sr)) {
+            float detected = 0.0f;
+#pragma unroll 4
+            for (int j = 0; j < nb; ++j)
+                detected = __fadd_rn(detected, ld_cluster(&bs_local[j / C][threadIdx.x], j % C));
+            result = __fadd_rn(result, __fmul_rn(detected, P.scale));
+        }
+        if (P.w)
+            result = __fmul_rn(result, w_v);
+        P.out[oidx] = result;
+    }
+    cluster_sync_all();
+}
+
+struct SartBpArgs {
+    const float *sino;
+    float *vol;             /* padded layout, [slices][rows][pitch] */
+    int n;
+    int angle;
+    int pitch;
+    float os, shift, e0, e1;
+    float sn, cs;
+    float relax;
+    float neg_zero;
+    const float *relax_dev;
+    int *err;
+    long long vol_stride;
+    long long sino_stride;
+};
+
+constexpr int kBpTileW = 128;   /* storage columns per CTA: 32 threads x 4 */
+constexpr int kBpSpan = 256;    /* sinogram values staged per CTA */
+
+/* The backprojection's detector coordinate of storage pixel (i, j), clamp
+ * excluded (…joseph.cl:189-195); with T the storage holds the transpose. */
+template <bool T>
+__device__ __forceinline__ float sart_bp_coord(const SartBpArgs &P, int i, int j)
+{
+    const float fI = __fsub_rn(__fadd_rn((float) i, 0.5f), P.os);
+    const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
+    const float fX = T ? fJ : fI;
+    const float fY = T ? fI : fJ;
+    return __fadd_rn(__fsub_rn(__fmul_rn(fX, P.cs), __fmul_rn(fY, P.sn)), P.shift);
+}
+
+/*
+ * vol = vol + relax * (0 + sample) for one angle on the padded layout
+ * (…joseph.cl:158-218 with a one-angle subset); requires e0 <= e1.
+ *
+ * A CTA updates an (8 ROWS) x 128 storage tile; thread (tx, ty) the columns
+ * tx + 32h (h = 0..3) of rows ty + 8m (m < ROWS), so the 32 lanes of a warp
+ * read 32 adjacent columns (coalesced) and, for one h, detector bins at most
+ * one apart (no shared-memory bank conflicts). Columns h and h + 1 form one
+ * packed pair. The coordinate is monotone in each pixel index (every
+ * rounding step is), so over the tile it lies between its values at the
+ * four corners (four lanes of each warp compute them): the CTA stages the
+ * sinogram values between those bounds in shared memory, and tiles whose
+ * corners lie within [e0, e1] skip the clamp. The row product is computed
+ * once per row, the column products once per thread.
+ * Grid (ceil(n/128), ceil(n/(8 ROWS)), slices), block 32 x 8.
+ */
+template <bool T, int ROWS>
+__global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
+{
+    __shared__ __align__(16) float rs[kBpSpan];
+    const int n = P.n;
+    const int lane = (int) threadIdx.x;
+    const int i_base = (int) blockIdx.x * kBpTileW, j_base = (int) blockIdx.y * (8 * ROWS);
+    /* lane k < 4 computes corner (k & 1, k >> 1); min and max over the four */
+    const int ci = (lane & 1) ? min(i_base + kBpTileW - 1, n - 1) : i_base;
+    const int cj = (lane & 2) ? min(j_base + 8 * ROWS - 1, n - 1) : j_base;
+    const float cc = sart_bp_coord<T>(P, ci, cj);
+    float umin = lane < 4 ? cc : INFINITY, umax = lane < 4 ? cc : -INFINITY;
+    umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, 1));
+    umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, 1));
+    umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, 2));
+    umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, 2));
+    umin = __shfl_sync(0xffffffffu, umin, 0);
+    umax = __shfl_sync(0xffffffffu, umax, 0);
+    const bool interior = umin >= P.e0 && umax <= P.e1;
+    const float cmin = fminf(fmaxf(umin, P.e0), P.e1), cmax = fminf(fmaxf(umax, P.e0), P.e1);
+    const int lo = (int) floorf(__fsub_rn(cmin, 0.5f));
+    const int span = (int) floorf(__fsub_rn(cmax, 0.5f)) + 2 - lo;
+    const int tid = (int) (threadIdx.y * 32 + threadIdx.x);
+    if (span > kBpSpan) {      /* cannot happen for |sin|, |cos| <= 1; uniform per CTA */
+        if (tid == 0)
+            atomicOr(P.err, kErrSpan);
+        return;
+    }
+    /* the tile's pixels first: their loads overlap the staging below */
+    const int i0 = i_base + lane;
+    bool okc[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h)
+        okc[h] = i0 + 32 * h < n;
+    float *vcol = P.vol + (size_t) blockIdx.z * P.vol_stride + (size_t) (j_base + (int) threadIdx.y) * P.pitch +
+                  kSartPadL + i0;
+    const int rows_left = n - j_base - (int) threadIdx.y;     /* rows m with 8m < rows_left exist */
+    float x[ROWS][4];
+#pragma unroll
+    for (int m = 0; m < ROWS; ++m) {
+        const float *row = vcol + (size_t) (8 * m) * P.pitch;
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+            x[m][h] = okc[h] && 8 * m < rows_left ? row[32 * h] : 0.0f;
+    }
+    const float *r = P.sino + (size_t) blockIdx.z * P.sino_stride + (size_t) P.angle * n;
+    for (int k = tid; k < span; k += 256) {
+        const int idx = lo + k;
+        rs[k] = (idx >= 0 && idx < n) ? __ldg(r + idx) : 0.0f;
+    }
+    __syncthreads();
+    if (!okc[0] || rows_left <= 0)
+        return;
+
+    const float relax = P.relax_dev ? *P.relax_dev : P.relax;
+    const float2 z2 = joseph::splat(P.neg_zero);
+    /* column products; columns past n repeat column n - 1 and are not stored */
+    float2 pc[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int ia = min(i0 + 64 * h, n - 1), ib = min(i0 + 64 * h + 32, n - 1);
+        const float2 fI = make_float2(__fsub_rn(__fadd_rn((float) ia, 0.5f), P.os),
+                                      __fsub_rn(__fadd_rn((float) ib, 0.5f), P.os));
+        pc[h] = joseph::mul2z(fI, joseph::splat(T ? P.sn : P.cs), z2);
+    }
+    const uint32_t rbase = (uint32_t) __cvta_generic_to_shared(rs) -
+                           4u * (uint32_t) (joseph::kHalfFloorBits + lo);
+#pragma unroll
+    for (int m = 0; m < ROWS; ++m) {
+        const int j = min(j_base + (int) threadIdx.y + 8 * m, n - 1);
+        const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
+        const float q = __fmul_rn(fJ, T ? P.cs : P.sn);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float2 d = T ? joseph::sub2(joseph::splat(q), pc[h]) : joseph::sub2(pc[h], joseph::splat(q));
+            float2 c = joseph::add2(d, joseph::splat(P.shift));
+            if (!interior)
+                c = make_float2(fminf(fmaxf(c.x, P.e0), P.e1), fminf(fmaxf(c.y, P.e0), P.e1));
+            float2 t;
+            const float2 y = joseph::floor_half2(c, t);
+            const uint32_t aa = rbase + 4u * (uint32_t) __float_as_int(y.x);
+            const uint32_t ab = rbase + 4u * (uint32_t) __float_as_int(y.y);
+            const float2 t0 = make_float2(joseph::lds(aa), joseph::lds(ab));
+            const float2 t1 = make_float2(joseph::lds(aa + 4u), joseph::lds(ab + 4u));
+            const float2 sum = joseph::add2(joseph::splat(0.0f), joseph::lerp2(t, t0, t1, z2));
+            const float2 upd = joseph::add2(make_float2(x[m][2 * h], x[m][2 * h + 1]),
+                                            joseph::mul2z(joseph::splat(relax), sum, z2));
+            x[m][2 * h] = upd.x;
+            x[m][2 * h + 1] = upd.y;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < ROWS; ++m) {
+        if (8 * m < rows_left) {
+            float *row = vcol + (size_t) (8 * m) * P.pitch;
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                if (okc[h])
+                    row[32 * h] = x[m][h];
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" size_t udev_fp_block_starts_floats(int n, int n_angles)
@@ -331,4 +735,174 @@ extern "C" int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, f
     else
         bp_angle_kernel<false><<<grid, dim3(32, 8), 0, d->stream>>>(A);
     return udev_after_launch(d, "bp_angle_kernel");
+}
+
+/* ---- the padded sweep layout ---- */
+
+extern "C" int udev_sart_pitch(int n)
+{
+    return sart_pitch(n);
+}
+
+extern "C" size_t udev_sart_work_floats(int n, int n_slices)
+{
+    const size_t plane = (size_t) sart_rows(n) * (size_t) sart_pitch(n);
+    return (size_t) n_slices * 2 * plane;
+}
+
+/* The clamp edges of the backprojection (…joseph.cl:174-187), computed as
+ * the host side of udev_bp_angle does. */
+static void sart_bp_consts(const udev_geom *g, float *os, float *shift, float *e0, float *e1)
+{
+    const float w = (float) g->n_dets, axis = g->axis;
+    const float required_width = axis * 2.0f;
+    const float diff = w - required_width;
+    const float ros = diff / 2.0f;
+    const float half = diff < 0.0f ? w - axis : axis;
+    *os = w / 2.0f;
+    *shift = *os - ros;
+    *e0 = axis - half + 0.5f;
+    *e1 = axis + half - 0.5f;
+}
+
+extern "C" int udev_sart_padded(const udev_geom *g)
+{
+    float os, shift, e0, e1;
+    if (g->n_dets < 1 || g->n_dets > kMaxBlocks * kBlock)
+        return 0;
+    sart_bp_consts(g, &os, &shift, &e0, &e1);
+    return e0 <= e1;
+}
+
+/* Copies between the user's n x n slices (place -1) and the padded copies
+ * V (place 0) and H (place 1, the transpose). */
+extern "C" int udev_sart_move(udev *d, int n, float *x, float *work, int from, int to, int n_slices)
+{
+    if (n_slices <= 0 || n <= 0)
+        return UFOIR_OK;
+    if (from == to || from < -1 || from > 1 || to < -1 || to > 1 || n_slices > 65535) {
+        udev_set_error(d, "sart_move: bad places %d -> %d or %d slices", from, to, n_slices);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    const int pitch = sart_pitch(n);
+    const long long plane = (long long) sart_rows(n) * pitch;
+    float *place[2] = {work, work + (size_t) n_slices * plane};
+    const float *src = from < 0 ? x : place[from];
+    float *dst = to < 0 ? x : place[to];
+    const int sp = from < 0 ? n : pitch, so = from < 0 ? 0 : kSartPadL;
+    const int dp = to < 0 ? n : pitch, dof = to < 0 ? 0 : kSartPadL;
+    const long long ss = from < 0 ? (long long) n * n : plane, ds = to < 0 ? (long long) n * n : plane;
+    /* H is the transpose of V and of the user's layout */
+    const int transpose = (from == 1) != (to == 1);
+    dim3 grid(udev_div_up(n, 32), udev_div_up(n, 32), (unsigned int) n_slices);
+    sart_copy_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(src, sp, so, ss, dst, dp, dof, ds, n, transpose);
+    return udev_after_launch(d, "sart_copy_kernel");
+}
+
+extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, const float *table, float *work,
+                            int place, const float *src, const float *w, int w_shared, float *out, float scale,
+                            int n_slices)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    const int n = g->n_dets;
+    if (angle < 0 || angle >= g->n_angles || n < 1 || n > kMaxBlocks * kBlock || n_slices > 65535 ||
+        (place != 0 && place != 1)) {
+        udev_set_error(d, "sart_fp: angle %d of %d, n = %d, %d slices, place %d out of range", angle, g->n_angles,
+                       n, n_slices, place);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    const int pitch = sart_pitch(n);
+    const size_t plane = (size_t) sart_rows(n) * pitch;
+    const int nb = (n + kBlock - 1) / kBlock, groups = (n + 63) / 64;
+    SartFpArgs A;
+    A.img = work + (size_t) place * n_slices * plane;
+    A.table = table;
+    A.src = src;
+    A.w = w;
+    A.out = out;
+    A.sinv = g->d_sin;
+    A.cosv = g->d_cos;
+    A.n = n;
+    A.n_blocks = nb;
+    A.angle = angle;
+    A.dir = dir;
+    A.pitch = pitch;
+    A.cluster = nb < kFpCluster ? nb : kFpCluster;
+    A.axis = g->axis;
+    A.scale = scale;
+    A.neg_zero = -0.0f;
+    A.img_stride = (long long) plane;
+    A.sino_stride = (long long) g->n_angles * n;
+    A.w_stride = w_shared ? 0 : A.sino_stride;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned int) (groups * A.cluster), 1, (unsigned int) n_slices);
+    cfg.blockDim = dim3(128, 1, 1);
+    cfg.stream = d->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned int) A.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    /* four segment warps per block while a CTA holds at most two blocks */
+    const int per_cta = udev_div_up(nb, A.cluster);
+    cudaError_t e = per_cta <= 2 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4>, A)
+                                 : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1>, A);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        udev_set_error(d, "sart_fp_kernel launch: %s", cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
+    }
+    return udev_after_launch(d, "sart_fp_kernel");
+}
+
+extern "C" int udev_sart_bp(udev *d, const udev_geom *g, int angle, float sn, float cs, const float *sino,
+                            float *work, int place, float relax, const float *relax_dev, int n_slices)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    const int n = g->n_dets;
+    if (angle < 0 || angle >= g->n_angles || n < 1 || n_slices > 65535 || (place != 0 && place != 1) ||
+        !udev_sart_padded(g)) {
+        udev_set_error(d, "sart_bp: angle %d of %d, n = %d, %d slices, place %d out of range", angle, g->n_angles,
+                       n, n_slices, place);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    const int pitch = sart_pitch(n);
+    const size_t plane = (size_t) sart_rows(n) * pitch;
+    SartBpArgs A;
+    sart_bp_consts(g, &A.os, &A.shift, &A.e0, &A.e1);
+    A.sino = sino;
+    A.vol = work + (size_t) place * n_slices * plane;
+    A.n = n;
+    A.angle = angle;
+    A.pitch = pitch;
+    A.sn = sn;
+    A.cs = cs;
+    A.relax = relax;
+    A.neg_zero = -0.0f;
+    A.relax_dev = relax_dev;
+    A.err = d->d_err;
+    A.vol_stride = (long long) plane;
+    A.sino_stride = (long long) g->n_angles * n;
+    /* 32-row tiles while they leave fewer than ~4 CTAs per SM, else 64-row */
+    const bool tall = (long long) udev_div_up(n, kBpTileW) * udev_div_up(n, 64) * n_slices >= 4LL * udev_sm_count(d);
+    dim3 grid(udev_div_up(n, kBpTileW), udev_div_up(n, tall ? 64 : 32), (unsigned int) n_slices);
+    if (tall) {
+        if (place == 1)
+            sart_bp_kernel<true, 8><<<grid, dim3(32, 8), 0, d->stream>>>(A);
+        else
+            sart_bp_kernel<false, 8><<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    } else {
+        if (place == 1)
+            sart_bp_kernel<true, 4><<<grid, dim3(32, 8), 0, d->stream>>>(A);
+        else
+            sart_bp_kernel<false, 4><<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    }
+    return udev_after_launch(d, "sart_bp_kernel");
 }
