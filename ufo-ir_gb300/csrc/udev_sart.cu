@@ -323,26 +323,25 @@ __device__ __forceinline__ void cluster_sync_all()
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-/* A float of CTA `rank`'s shared memory, at the address `local` has here. */
+/* A float of CTA `rank`'s shared memory, at the address `local` has here.
+ * Ordering against the writes comes from the cluster barrier before it, so
+ * the loads may be issued back to back. */
 __device__ __forceinline__ float ld_cluster(const float *local, int rank)
 {
     uint32_t remote;
     float v;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
-                 : "=r"(remote)
-                 : "r"((uint32_t) __cvta_generic_to_shared(local)), "r"(rank));
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(remote) : "memory");
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"((uint32_t) __cvta_generic_to_shared(local)), "r"(rank));
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(remote));
     return v;
 }
 
-/* The samples [row0, row0 + rows) of rays (s0, s1) of one block, from the
- * coordinates c at row0: appends them to the running sum (Q == 1) or
- * stores them in v (Q > 1). All loads of 16 samples are in flight together. */
-template <int ROWS, bool STREAM>
+/* The samples [row0, row0 + ROWS) of rays (s0, s1) of one block, from the
+ * coordinates c at row0, in batches of K samples whose loads are all in
+ * flight together: appended to the running sum (STREAM) or stored in v. */
+template <int ROWS, int K, bool STREAM>
 __device__ __forceinline__ void sart_fp_samples(const float *img, int pitch, float2 c, float2 st, float hi,
                                                 float2 z2, float2 &run, float2 *v)
 {
-    constexpr int K = 16;
 #pragma unroll 1
     for (int k0 = 0; k0 < ROWS; k0 += K) {
         float2 t[K];
@@ -393,8 +392,8 @@ __device__ __forceinline__ void sart_fp_samples(const float *img, int pitch, flo
  * shared memory alive until then. Grid (groups * C, 1, slices), cluster
  * (C, 1, 1), 128 threads.
  */
-template <int SEG>
-__global__ void __launch_bounds__(128, 3) sart_fp_kernel(SartFpArgs P)
+template <int SEG, int K, int W, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) sart_fp_kernel(SartFpArgs P)
 {
     __shared__ float bs_local[kFpLocal][64];
     __shared__ float2 run_s[32];
@@ -432,7 +431,7 @@ __global__ void __launch_bounds__(128, 3) sart_fp_kernel(SartFpArgs P)
             for (int k = 0; k < 16 * warp; ++k)
                 c = joseph::add2(c, st);
             float2 v[16], run = joseph::splat(0.0f);
-            sart_fp_samples<16, false>(img0 + (size_t) (b * kBlock + 16 * warp) * P.pitch, P.pitch, c, st, hi, z2,
+            sart_fp_samples<16, 16, false>(img0 + (size_t) (b * kBlock + 16 * warp) * P.pitch, P.pitch, c, st, hi, z2,
                                        run, v);
             /* inner = (((0 + v_0) + v_1) + ... + v_63), segment by segment */
 #pragma unroll
@@ -454,12 +453,12 @@ __global__ void __launch_bounds__(128, 3) sart_fp_kernel(SartFpArgs P)
             }
         }
     } else {
-        for (int i = warp; rank + C * i < nb; i += 4) {
+        for (int i = warp; rank + C * i < nb; i += W) {
             const int b = rank + C * i;
             const float *tb = tab + (size_t) b * n;
             const float2 c = make_float2(__ldg(tb + min(s0, n - 1)), __ldg(tb + min(s1, n - 1)));
             float2 run = joseph::splat(0.0f);
-            sart_fp_samples<kBlock, true>(img0 + (size_t) b * kBlock * P.pitch, P.pitch, c, st, hi, z2, run,
+            sart_fp_samples<kBlock, K, true>(img0 + (size_t) b * kBlock * P.pitch, P.pitch, c, st, hi, z2, run,
                                           nullptr);
             bs_local[i][lane] = run.x;
             bs_local[i][lane + 32] = run.y;
@@ -470,10 +469,20 @@ __global__ void __launch_bounds__(128, 3) sart_fp_kernel(SartFpArgs P)
         float result = src_v;
         const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
         if (!joseph::detector_inactive(kc, sr)) {
+            /* block sums in block order; eight remote loads in flight at a time */
             float detected = 0.0f;
-#pragma unroll 4
-            for (int j = 0; j < nb; ++j)
-                detected = __fadd_rn(detected, ld_cluster(&bs_local[j / C][threadIdx.x], j % C));
+            for (int j0 = 0; j0 < nb; j0 += 8) {
+                float bsv[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int j = min(j0 + k, nb - 1);
+                    bsv[k] = ld_cluster(&bs_local[j / C][threadIdx.x], j % C);
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (j0 + k < nb)
+                        detected = __fadd_rn(detected, bsv[k]);
+            }
             result = __fadd_rn(result, __fmul_rn(detected, P.scale));
         }
         if (P.w)
@@ -830,16 +839,36 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     A.angle = angle;
     A.dir = dir;
     A.pitch = pitch;
-    A.cluster = nb < kFpCluster ? nb : kFpCluster;
     A.axis = g->axis;
     A.scale = scale;
     A.neg_zero = -0.0f;
     A.img_stride = (long long) plane;
     A.sino_stride = (long long) g->n_angles * n;
     A.w_stride = w_shared ? 0 : A.sino_stride;
+    /* Launch shape: up to 16 blocks, clusters of up to 8 CTAs with one or
+     * two blocks each, four segment warps (16 rows each) per block; else,
+     * where it fits in one wave, one
+     * block per warp: 16-sample batches in 4-warp CTAs (3 per SM), or
+     * 8-sample batches in 8-warp CTAs (2 per SM, fewer registers); else
+     * clusters of 8 CTAs with several blocks per warp. */
+    const long long sms = udev_sm_count(d);
+    int shape;
+    if (nb <= 2 * kFpCluster) {
+        shape = 0;
+        A.cluster = nb < kFpCluster ? nb : kFpCluster;
+    } else if (udev_div_up(nb, 4) <= kFpCluster && (long long) groups * udev_div_up(nb, 4) * n_slices <= 3 * sms) {
+        shape = 1;
+        A.cluster = (int) udev_div_up(nb, 4);
+    } else if (udev_div_up(nb, 8) <= kFpCluster && (long long) groups * udev_div_up(nb, 8) * n_slices <= 2 * sms) {
+        shape = 2;
+        A.cluster = (int) udev_div_up(nb, 8);
+    } else {
+        shape = 1;
+        A.cluster = kFpCluster;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned int) (groups * A.cluster), 1, (unsigned int) n_slices);
-    cfg.blockDim = dim3(128, 1, 1);
+    cfg.blockDim = dim3(shape == 2 ? 256 : 128, 1, 1);
     cfg.stream = d->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -848,10 +877,9 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    /* four segment warps per block while a CTA holds at most two blocks */
-    const int per_cta = udev_div_up(nb, A.cluster);
-    cudaError_t e = per_cta <= 2 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4>, A)
-                                 : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1>, A);
+    cudaError_t e = shape == 0   ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4, 16, 4, 3>, A)
+                    : shape == 1 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 16, 4, 3>, A)
+                                 : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 8, 2>, A);
     if (e != cudaSuccess) {
         cudaGetLastError();
         udev_set_error(d, "sart_fp_kernel launch: %s", cudaGetErrorString(e));
