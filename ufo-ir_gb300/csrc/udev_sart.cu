@@ -849,8 +849,9 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
      * two blocks each, four segment warps (16 rows each) per block; else,
      * where it fits in one wave, one
      * block per warp: 16-sample batches in 4-warp CTAs (3 per SM), or
-     * 8-sample batches in 8-warp CTAs (2 per SM, fewer registers); else
-     * clusters of 8 CTAs with several blocks per warp. */
+     * 8-sample batches (fewer registers) in 16-warp CTAs (one per SM) or
+     * 8-warp CTAs (2 per SM); else clusters of 8 CTAs with several blocks
+     * per warp. */
     const long long sms = udev_sm_count(d);
     int shape;
     if (nb <= 2 * kFpCluster) {
@@ -859,6 +860,9 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     } else if (udev_div_up(nb, 4) <= kFpCluster && (long long) groups * udev_div_up(nb, 4) * n_slices <= 3 * sms) {
         shape = 1;
         A.cluster = (int) udev_div_up(nb, 4);
+    } else if (udev_div_up(nb, 16) <= kFpCluster && (long long) groups * udev_div_up(nb, 16) * n_slices <= sms) {
+        shape = 3;
+        A.cluster = (int) udev_div_up(nb, 16);
     } else if (udev_div_up(nb, 8) <= kFpCluster && (long long) groups * udev_div_up(nb, 8) * n_slices <= 2 * sms) {
         shape = 2;
         A.cluster = (int) udev_div_up(nb, 8);
@@ -868,7 +872,7 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned int) (groups * A.cluster), 1, (unsigned int) n_slices);
-    cfg.blockDim = dim3(shape == 2 ? 256 : 128, 1, 1);
+    cfg.blockDim = dim3(shape == 3 ? 512 : shape == 2 ? 256 : 128, 1, 1);
     cfg.stream = d->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -879,7 +883,8 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     cfg.numAttrs = 1;
     cudaError_t e = shape == 0   ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4, 16, 4, 3>, A)
                     : shape == 1 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 16, 4, 3>, A)
-                                 : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 8, 2>, A);
+                    : shape == 2 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 8, 2>, A)
+                                 : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 16, 1>, A);
     if (e != cudaSuccess) {
         cudaGetLastError();
         udev_set_error(d, "sart_fp_kernel launch: %s", cudaGetErrorString(e));
