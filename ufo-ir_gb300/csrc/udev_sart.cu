@@ -523,6 +523,39 @@ __device__ __forceinline__ float sart_bp_coord(const SartBpArgs &P, int i, int j
     return __fadd_rn(__fsub_rn(__fmul_rn(fX, P.cs), __fmul_rn(fY, P.sn)), P.shift);
 }
 
+/* The pixel updates of one thread: rows j0 + 8m (m < ROWS, clamped to the
+ * image), column pairs with products pc; CLAMP for tiles that reach past
+ * the clamp edges. */
+template <bool T, int ROWS, bool CLAMP>
+__device__ __forceinline__ void sart_bp_rows(const SartBpArgs &P, float (&x)[ROWS][4], const float2 (&pc)[2],
+                                             int j0, uint32_t rbase, float relax, float2 z2)
+{
+#pragma unroll
+    for (int m = 0; m < ROWS; ++m) {
+        const int j = min(j0 + 8 * m, P.n - 1);
+        const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
+        const float q = __fmul_rn(fJ, T ? P.cs : P.sn);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float2 d = T ? joseph::sub2(joseph::splat(q), pc[h]) : joseph::sub2(pc[h], joseph::splat(q));
+            float2 c = joseph::add2(d, joseph::splat(P.shift));
+            if (CLAMP)
+                c = make_float2(fminf(fmaxf(c.x, P.e0), P.e1), fminf(fmaxf(c.y, P.e0), P.e1));
+            float2 t;
+            const float2 y = joseph::floor_half2(c, t);
+            const uint32_t aa = rbase + 4u * (uint32_t) __float_as_int(y.x);
+            const uint32_t ab = rbase + 4u * (uint32_t) __float_as_int(y.y);
+            const float2 t0 = make_float2(joseph::lds(aa), joseph::lds(ab));
+            const float2 t1 = make_float2(joseph::lds(aa + 4u), joseph::lds(ab + 4u));
+            const float2 sum = joseph::add2(joseph::splat(0.0f), joseph::lerp2(t, t0, t1, z2));
+            const float2 upd = joseph::add2(make_float2(x[m][2 * h], x[m][2 * h + 1]),
+                                            joseph::mul2z(joseph::splat(relax), sum, z2));
+            x[m][2 * h] = upd.x;
+            x[m][2 * h + 1] = upd.y;
+        }
+    }
+}
+
 /*
  * vol = vol + relax * (0 + sample) for one angle on the padded layout
  * (…joseph.cl:158-218 with a one-angle subset); requires e0 <= e1.
@@ -606,30 +639,11 @@ __global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
     }
     const uint32_t rbase = (uint32_t) __cvta_generic_to_shared(rs) -
                            4u * (uint32_t) (joseph::kHalfFloorBits + lo);
-#pragma unroll
-    for (int m = 0; m < ROWS; ++m) {
-        const int j = min(j_base + (int) threadIdx.y + 8 * m, n - 1);
-        const float fJ = __fsub_rn(__fadd_rn((float) j, 0.5f), P.os);
-        const float q = __fmul_rn(fJ, T ? P.cs : P.sn);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const float2 d = T ? joseph::sub2(joseph::splat(q), pc[h]) : joseph::sub2(pc[h], joseph::splat(q));
-            float2 c = joseph::add2(d, joseph::splat(P.shift));
-            if (!interior)
-                c = make_float2(fminf(fmaxf(c.x, P.e0), P.e1), fminf(fmaxf(c.y, P.e0), P.e1));
-            float2 t;
-            const float2 y = joseph::floor_half2(c, t);
-            const uint32_t aa = rbase + 4u * (uint32_t) __float_as_int(y.x);
-            const uint32_t ab = rbase + 4u * (uint32_t) __float_as_int(y.y);
-            const float2 t0 = make_float2(joseph::lds(aa), joseph::lds(ab));
-            const float2 t1 = make_float2(joseph::lds(aa + 4u), joseph::lds(ab + 4u));
-            const float2 sum = joseph::add2(joseph::splat(0.0f), joseph::lerp2(t, t0, t1, z2));
-            const float2 upd = joseph::add2(make_float2(x[m][2 * h], x[m][2 * h + 1]),
-                                            joseph::mul2z(joseph::splat(relax), sum, z2));
-            x[m][2 * h] = upd.x;
-            x[m][2 * h + 1] = upd.y;
-        }
-    }
+    const int j0 = j_base + (int) threadIdx.y;
+    if (interior)
+        sart_bp_rows<T, ROWS, false>(P, x, pc, j0, rbase, relax, z2);
+    else
+        sart_bp_rows<T, ROWS, true>(P, x, pc, j0, rbase, relax, z2);
 #pragma unroll
     for (int m = 0; m < ROWS; ++m) {
         if (8 * m < rows_left) {
