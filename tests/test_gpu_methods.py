@@ -60,11 +60,14 @@ def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, sli
 
 
 # Sizes above 512 detectors split a ray's 64-sample blocks over several CTAs
-# of the per-angle forward projection (the last CTA adds the block sums);
-# off-centre axes give inactive detectors and clamped backprojection tiles.
+# of the per-angle forward projection (a cluster whose CTA 0 adds the block
+# sums), with a launch shape per size: 16-row segments (n <= 1024), one block
+# per warp (1111, 1448, 2900), several blocks per warp (2900 x 2 slices,
+# 4100); off-centre axes give inactive detectors and clamped tiles.
 @pytest.mark.parametrize("n,na,axis,iters,slices", [(513, 24, -1.0, 1, 1), (600, 40, 290.6, 2, 2),
                                                      (1111, 30, -1.0, 1, 1), (1448, 36, 700.25, 1, 1),
-                                                     (2900, 12, -1.0, 1, 1)])
+                                                     (2900, 12, -1.0, 1, 1), (2900, 6, 1449.5, 1, 2),
+                                                     (4100, 6, -1.0, 1, 1)])
 def test_sart_chunked_sizes_match_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
     rng = np.random.default_rng(5 * n + na)
     step = np.float32(np.pi / na)
