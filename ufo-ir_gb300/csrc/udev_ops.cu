@@ -85,30 +85,47 @@ __device__ __forceinline__ float tex0(const float *img, int x, int y, int w, int
     return (x >= 0 && y >= 0 && x < w && y < h) ? img[(size_t) y * w + x] : 0.0f;
 }
 
-/* l1_grad: 7-point isotropic-TV subgradient with EPS 0.001 and zero border. */
-__global__ void l1_grad_kernel(const float *in, float *out, int w, int h, long long stride)
+/* l1_grad: 7-point isotropic-TV subgradient with EPS 0.001 and zero border.
+ * A block computes a 32 x 32 tile, 4 rows per thread, from the tile and its
+ * one-pixel halo staged in shared memory (zeros outside the image). */
+constexpr int kGradTile = 32;
+
+__global__ void __launch_bounds__(256) l1_grad_kernel(const float *in, float *out, int w, int h, long long stride)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= w || y >= h)
-        return;
+    __shared__ float t[kGradTile + 2][kGradTile + 3];
+    const int x0 = (int) blockIdx.x * kGradTile, y0 = (int) blockIdx.y * kGradTile;
     const float *img = in + (size_t) blockIdx.z * stride;
-    const float f3 = tex0(img, x, y, w, h);
-    const float f1 = tex0(img, x, y - 1, w, h);
-    const float f0 = tex0(img, x - 1, y - 1, w, h);
-    const float f2 = tex0(img, x - 1, y, w, h);
-    const float f4 = tex0(img, x + 1, y, w, h);
-    const float f6 = tex0(img, x + 1, y + 1, w, h);
-    const float f5 = tex0(img, x, y + 1, w, h);
+    const int tid = (int) (threadIdx.y * 32 + threadIdx.x);
+    for (int e = tid; e < (kGradTile + 2) * (kGradTile + 2); e += 256) {
+        const int ty = e / (kGradTile + 2), tx = e % (kGradTile + 2);
+        t[ty][tx] = tex0(img, x0 - 1 + tx, y0 - 1 + ty, w, h);
+    }
+    __syncthreads();
+    const int lx = (int) threadIdx.x + 1, x = x0 + (int) threadIdx.x;
+    if (x >= w)
+        return;
     const float eps = 0.001f;
-    const float d32 = __fsub_rn(f3, f2), d35 = __fsub_rn(f3, f5);
-    const float d43 = __fsub_rn(f4, f3), d46 = __fsub_rn(f4, f6);
-    const float d13 = __fsub_rn(f1, f3), d10 = __fsub_rn(f1, f0);
-    const float t1 = __fdiv_rn(__fsub_rn(__fsub_rn(__fmul_rn(2.0f, f3), f2), f5),
-                               __fsqrt_rn(__fadd_rn(__fadd_rn(eps, __fmul_rn(d32, d32)), __fmul_rn(d35, d35))));
-    const float t2 = __fdiv_rn(d43, __fsqrt_rn(__fadd_rn(__fadd_rn(eps, __fmul_rn(d43, d43)), __fmul_rn(d46, d46))));
-    const float t3 = __fdiv_rn(d13, __fsqrt_rn(__fadd_rn(__fadd_rn(eps, __fmul_rn(d13, d13)), __fmul_rn(d10, d10))));
-    out[(size_t) blockIdx.z * stride + (size_t) y * w + x] = __fsub_rn(__fsub_rn(t1, t2), t3);
+#pragma unroll
+    for (int m = 0; m < kGradTile / 8; ++m) {
+        const int ly = (int) threadIdx.y + 8 * m + 1, y = y0 + ly - 1;
+        if (y >= h)
+            break;
+        const float f3 = t[ly][lx];
+        const float f1 = t[ly - 1][lx];
+        const float f0 = t[ly - 1][lx - 1];
+        const float f2 = t[ly][lx - 1];
+        const float f4 = t[ly][lx + 1];
+        const float f6 = t[ly + 1][lx + 1];
+        const float f5 = t[ly + 1][lx];
+        const float d32 = __fsub_rn(f3, f2), d35 = __fsub_rn(f3, f5);
+        const float d43 = __fsub_rn(f4, f3), d46 = __fsub_rn(f4, f6);
+        const float d13 = __fsub_rn(f1, f3), d10 = __fsub_rn(f1, f0);
+        const float t1 = __fdiv_rn(__fsub_rn(__fsub_rn(__fmul_rn(2.0f, f3), f2), f5),
+                                   __fsqrt_rn(__fadd_rn(__fadd_rn(eps, __fmul_rn(d32, d32)), __fmul_rn(d35, d35))));
+        const float t2 = __fdiv_rn(d43, __fsqrt_rn(__fadd_rn(__fadd_rn(eps, __fmul_rn(d43, d43)), __fmul_rn(d46, d46))));
+        const float t3 = __fdiv_rn(d13, __fsqrt_rn(__fadd_rn(__fadd_rn(eps, __fmul_rn(d13, d13)), __fmul_rn(d10, d10))));
+        out[(size_t) blockIdx.z * stride + (size_t) y * w + x] = __fsub_rn(__fsub_rn(t1, t2), t3);
+    }
 }
 
 template <int WHICH>
@@ -333,7 +350,7 @@ extern "C" int udev_l1_grad(udev *d, const float *in, float *out, int w, int h, 
     if (n_slices <= 0)
         return UFOIR_OK;
     UDEV_BIND(d);
-    dim3 grid(udev_div_up(w, 32), udev_div_up(h, 8), (unsigned int) n_slices);
+    dim3 grid(udev_div_up(w, kGradTile), udev_div_up(h, kGradTile), (unsigned int) n_slices);
     l1_grad_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(in, out, w, h, (long long) w * h);
     return udev_after_launch(d, "l1_grad_kernel");
 }
