@@ -6,7 +6,8 @@
  * (x0 + tx, y0 + ty + 8p), p < 16, which share fX * cos(theta) and the
  * per-angle set-up (16 pixels amortise it better than 8: 2.3 % on the C2
  * backprojection; 32 pixels, 32 x 256 tiles, need 139 KB of shared memory
- * and 132 registers, one CTA per SM, and were 23 % slower). For a chunk of
+ * and 132 registers, one CTA per SM, and were 23 % slower; a 64-register
+ * build with 16-angle chunks, four CTAs per SM, was 6 % slower). For a chunk of
  * 32 angles the CTA copies, per angle, the
  * 160 detector values that the tile can reach (cp.async, double buffered;
  * detectors outside [0, n) read 0), so every sample reads shared memory and
