@@ -390,7 +390,7 @@ __device__ __forceinline__ void sart_fp_samples(const float *img, int pitch, flo
  * over distributed shared memory, adds them in block order and writes the
  * rays' results (…joseph.cl:93-100); a second barrier keeps every CTA's
  * shared memory alive until then. Grid (groups * C, 1, slices), cluster
- * (C, 1, 1), 128 threads.
+ * (C, 1, 1), 32 W threads; K samples per batch of loads.
  */
 template <int SEG, int K, int W, int MINB>
 __global__ void __launch_bounds__(32 * W, MINB) sart_fp_kernel(SartFpArgs P)
