@@ -411,6 +411,10 @@ UFOIR_API int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, 
 /* sample instruction sequence run from shared memory by every SM with no   */
 /* global traffic. Projector sample rates are reported against it.          */
 UFOIR_API int ufoir_sample_ceiling(ufoir_ctx *ctx, double *samples_per_s);
+/* The same for the backprojector's per-sample sequence (per angle: the     */
+/* angle record and row products from shared memory; per pixel pair: the   */
+/* coordinate, floor, two window taps per pixel, filter and sum).          */
+UFOIR_API int ufoir_sample_ceiling_bp(ufoir_ctx *ctx, double *samples_per_s);
 
 #define UFOIR_NOALLOC_MAX_SLICES 64
 UFOIR_API int ufoir_l1_norm_fp64_noalloc(const float *d_v, size_t count, unsigned int n_slices,

@@ -268,3 +268,12 @@ def test_errors_are_reported_not_fatal(ufoir_lib, gpu_ctx):
     # the context is still usable
     out = p.forward(np.ones((8, 8), np.float32), np.zeros((4, 8), np.float32))
     assert np.isfinite(out).all()
+
+
+def test_sample_ceilings_are_measured(gpu_ctx):
+    # each projector's per-sample sequence from shared memory: some 1e12
+    # samples/s on a GB300, the backprojector's close to the forward one's
+    fp = gpu_ctx.sample_ceiling()
+    bp = gpu_ctx.sample_ceiling_bp()
+    assert 1e11 < fp < 1e14 and 1e11 < bp < 1e14
+    assert 0.5 < bp / fp < 2.0

@@ -198,3 +198,10 @@ int ufoir_sample_ceiling(ufoir_ctx *ctx, double *samples_per_s)
         return UFOIR_ERR_INVALID;
     return udev_sample_ceiling(ctx->dev, samples_per_s);
 }
+
+int ufoir_sample_ceiling_bp(ufoir_ctx *ctx, double *samples_per_s)
+{
+    if (!ctx || !samples_per_s)
+        return UFOIR_ERR_INVALID;
+    return udev_sample_ceiling_bp(ctx->dev, samples_per_s);
+}

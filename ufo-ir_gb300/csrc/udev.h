@@ -69,6 +69,8 @@ int udev_transpose(udev *d, const float *in, float *out, int n, int n_slices);
 /* Interpolated samples/s of the forward projector's per-sample sequence run
  * from shared memory on every SM with no global traffic (udev_ceiling.cu). */
 int udev_sample_ceiling(udev *d, double *samples_per_s);
+/* The same for the backprojector's per-sample sequence. */
+int udev_sample_ceiling_bp(udev *d, double *samples_per_s);
 
 /* ---- Per-angle projections of a SART sweep (udev_sart.cu) ---- */
 /* Floats of the block-start table: the coordinate of every ray of every

@@ -134,7 +134,7 @@ EXPORTED = (
     "ufoir_serve_submit", "ufoir_serve_poll", "ufoir_serve_wait", "ufoir_serve_cancel", "ufoir_serve_drain",
     "ufoir_serve_get_stats", "ufoir_serve_destroy", "ufoir_graph_parse", "ufoir_graph_load",
     "ufoir_graph_job_desc", "ufoir_graph_run", "ufoir_io_last_error", "ufoir_io_tiff_info", "ufoir_io_read_tiff",
-    "ufoir_io_write_tiff", "ufoir_io_read_raw", "ufoir_io_write_raw", "ufoir_sample_ceiling",
+    "ufoir_io_write_tiff", "ufoir_io_read_raw", "ufoir_io_write_raw", "ufoir_sample_ceiling", "ufoir_sample_ceiling_bp",
 )
 
 
@@ -225,6 +225,7 @@ def _declare(L):
     L.ufoir_io_read_raw.argtypes = [C.c_char_p, C.c_uint64, vp, C.c_size_t]
     L.ufoir_io_write_raw.argtypes = [C.c_char_p, vp, C.c_size_t]
     L.ufoir_sample_ceiling.argtypes = [vp, C.POINTER(C.c_double)]
+    L.ufoir_sample_ceiling_bp.argtypes = [vp, C.POINTER(C.c_double)]
     L.ufoir_l1_norm.argtypes = [vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
     L.ufoir_dot_product.argtypes = [vp, vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
 
@@ -333,6 +334,12 @@ class Context:
         """Interpolated samples/s of the forward projector's per-sample sequence, no global traffic."""
         v = C.c_double()
         self._check(lib().ufoir_sample_ceiling(self.handle, C.byref(v)))
+        return v.value
+
+    def sample_ceiling_bp(self) -> float:
+        """Interpolated samples/s of the backprojector's per-sample sequence, no global traffic."""
+        v = C.c_double()
+        self._check(lib().ufoir_sample_ceiling_bp(self.handle, C.byref(v)))
         return v.value
 
     def pinned_empty(self, shape):
