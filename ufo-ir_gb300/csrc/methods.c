@@ -382,7 +382,7 @@ int ufoir__sart_body(void *arg)
      * x = x + lambda A_theta^T r_theta. The volume lives in the layout of the
      * current direction run, transposed while the angles are horizontal, so
      * that every ray walks rows. */
-    if (udev_sart_padded(&s->g)) {
+    if (udev_sart_padded(d, &s->g, S)) {
         /* padded copies V (vertical run) and H (horizontal run) in s->work */
         int place = -1;
         for (unsigned int a = 0; a < s->p->n_angles && rc == UFOIR_OK; a++) {

@@ -93,8 +93,9 @@ int udev_bp_angle(udev *d, const udev_geom *g, int angle, float sn, float cs, co
  * area (udev_sart_work_floats floats) must be zero-filled once. */
 int udev_sart_pitch(int n);
 size_t udev_sart_work_floats(int n, int n_slices);
-/* 1 if the padded kernels serve this geometry (clamp edges e0 <= e1). */
-int udev_sart_padded(const udev_geom *g);
+/* 1 if the padded kernels serve this geometry (clamp edges e0 <= e1) for
+ * n_slices slices on this GPU (a cluster of the forward projection fits). */
+int udev_sart_padded(udev *d, const udev_geom *g, int n_slices);
 /* Copies the volume between the user's slices (place -1), V (0) and H (1). */
 int udev_sart_move(udev *d, int n, float *x, float *work, int from, int to, int n_slices);
 /* udev_fp_angle and udev_bp_angle on the padded copy `place` (0 V for

@@ -788,13 +788,85 @@ static void sart_bp_consts(const udev_geom *g, float *os, float *shift, float *e
     *e1 = axis + half - 0.5f;
 }
 
-extern "C" int udev_sart_padded(const udev_geom *g)
+/* The padded kernels' arithmetic needs e0 <= e1 and n <= 8192. */
+static bool sart_geometry_ok(const udev_geom *g)
 {
     float os, shift, e0, e1;
     if (g->n_dets < 1 || g->n_dets > kMaxBlocks * kBlock)
-        return 0;
+        return false;
     sart_bp_consts(g, &os, &shift, &e0, &e1);
     return e0 <= e1;
+}
+
+/* Launch shape of the one-angle forward projection: up to 16 blocks,
+ * clusters of up to 8 CTAs with one or two blocks each, four segment warps
+ * (16 rows each) per block; else, where it fits in one wave, one block per
+ * warp: 16-sample batches in 4-warp CTAs (3 per SM), or 8-sample batches
+ * (fewer registers) in 16-warp CTAs (one per SM) or 8-warp CTAs (2 per
+ * SM); else clusters of 8 CTAs with several blocks per warp. */
+struct SartFpShape {
+    int shape;      /* 0: segments; 1, 2, 3: whole blocks per warp (4, 8, 16 warps per CTA) */
+    int cluster;
+    int threads;
+    const void *func;
+};
+
+static SartFpShape sart_fp_shape(udev *d, int n, int n_slices)
+{
+    const int nb = (n + kBlock - 1) / kBlock, groups = (n + 63) / 64;
+    const long long sms = udev_sm_count(d);
+    SartFpShape f;
+    if (nb <= 2 * kFpCluster) {
+        f.shape = 0;
+        f.cluster = nb < kFpCluster ? nb : kFpCluster;
+    } else if (udev_div_up(nb, 4) <= kFpCluster && (long long) groups * udev_div_up(nb, 4) * n_slices <= 3 * sms) {
+        f.shape = 1;
+        f.cluster = (int) udev_div_up(nb, 4);
+    } else if (udev_div_up(nb, 16) <= kFpCluster && (long long) groups * udev_div_up(nb, 16) * n_slices <= sms) {
+        f.shape = 3;
+        f.cluster = (int) udev_div_up(nb, 16);
+    } else if (udev_div_up(nb, 8) <= kFpCluster && (long long) groups * udev_div_up(nb, 8) * n_slices <= 2 * sms) {
+        f.shape = 2;
+        f.cluster = (int) udev_div_up(nb, 8);
+    } else {
+        f.shape = 1;
+        f.cluster = kFpCluster;
+    }
+    f.threads = f.shape == 3 ? 512 : f.shape == 2 ? 256 : 128;
+    f.func = f.shape == 0   ? (const void *) sart_fp_kernel<4, 16, 4, 3>
+             : f.shape == 1 ? (const void *) sart_fp_kernel<1, 16, 4, 3>
+             : f.shape == 2 ? (const void *) sart_fp_kernel<1, 8, 8, 2>
+                            : (const void *) sart_fp_kernel<1, 8, 16, 1>;
+    return f;
+}
+
+extern "C" int udev_sart_padded(udev *d, const udev_geom *g, int n_slices)
+{
+    if (!sart_geometry_ok(g) || n_slices < 1 || n_slices > 65535)
+        return 0;
+    /* one cluster of the forward projection's shape must fit on this GPU
+     * (a partition with few SMs may not hold it) */
+    if (cudaSetDevice(d->device) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const SartFpShape f = sart_fp_shape(d, g->n_dets, n_slices);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned int) f.cluster, 1, 1);
+    cfg.blockDim = dim3((unsigned int) f.threads, 1, 1);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned int) f.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, f.func, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return clusters > 0;
 }
 
 /* Copies between the user's n x n slices (place -1) and the padded copies
@@ -859,34 +931,11 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     A.img_stride = (long long) plane;
     A.sino_stride = (long long) g->n_angles * n;
     A.w_stride = w_shared ? 0 : A.sino_stride;
-    /* Launch shape: up to 16 blocks, clusters of up to 8 CTAs with one or
-     * two blocks each, four segment warps (16 rows each) per block; else,
-     * where it fits in one wave, one
-     * block per warp: 16-sample batches in 4-warp CTAs (3 per SM), or
-     * 8-sample batches (fewer registers) in 16-warp CTAs (one per SM) or
-     * 8-warp CTAs (2 per SM); else clusters of 8 CTAs with several blocks
-     * per warp. */
-    const long long sms = udev_sm_count(d);
-    int shape;
-    if (nb <= 2 * kFpCluster) {
-        shape = 0;
-        A.cluster = nb < kFpCluster ? nb : kFpCluster;
-    } else if (udev_div_up(nb, 4) <= kFpCluster && (long long) groups * udev_div_up(nb, 4) * n_slices <= 3 * sms) {
-        shape = 1;
-        A.cluster = (int) udev_div_up(nb, 4);
-    } else if (udev_div_up(nb, 16) <= kFpCluster && (long long) groups * udev_div_up(nb, 16) * n_slices <= sms) {
-        shape = 3;
-        A.cluster = (int) udev_div_up(nb, 16);
-    } else if (udev_div_up(nb, 8) <= kFpCluster && (long long) groups * udev_div_up(nb, 8) * n_slices <= 2 * sms) {
-        shape = 2;
-        A.cluster = (int) udev_div_up(nb, 8);
-    } else {
-        shape = 1;
-        A.cluster = kFpCluster;
-    }
+    const SartFpShape f = sart_fp_shape(d, n, n_slices);
+    A.cluster = f.cluster;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned int) (groups * A.cluster), 1, (unsigned int) n_slices);
-    cfg.blockDim = dim3(shape == 3 ? 512 : shape == 2 ? 256 : 128, 1, 1);
+    cfg.blockDim = dim3((unsigned int) f.threads, 1, 1);
     cfg.stream = d->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -895,10 +944,10 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = shape == 0   ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4, 16, 4, 3>, A)
-                    : shape == 1 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 16, 4, 3>, A)
-                    : shape == 2 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 8, 2>, A)
-                                 : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 16, 1>, A);
+    cudaError_t e = f.shape == 0   ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4, 16, 4, 3>, A)
+                    : f.shape == 1 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 16, 4, 3>, A)
+                    : f.shape == 2 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 8, 2>, A)
+                                   : cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 16, 1>, A);
     if (e != cudaSuccess) {
         cudaGetLastError();
         udev_set_error(d, "sart_fp_kernel launch: %s", cudaGetErrorString(e));
@@ -914,7 +963,7 @@ extern "C" int udev_sart_bp(udev *d, const udev_geom *g, int angle, float sn, fl
         return UFOIR_OK;
     const int n = g->n_dets;
     if (angle < 0 || angle >= g->n_angles || n < 1 || n_slices > 65535 || (place != 0 && place != 1) ||
-        !udev_sart_padded(g)) {
+        !sart_geometry_ok(g)) {
         udev_set_error(d, "sart_bp: angle %d of %d, n = %d, %d slices, place %d out of range", angle, g->n_angles,
                        n, n_slices, place);
         return UFOIR_ERR_INVALID;
