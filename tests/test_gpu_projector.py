@@ -205,10 +205,13 @@ def test_full_size_bp_matches_oracle_on_a_row_band(ufoir_lib, gpu_ctx, oracle):
     assert rel_l2(gb, wb) <= TOL_ONE and np.array_equal(gb, wb)
 
 
-@pytest.mark.parametrize("n,na,axis,slices", [(1448, 48, -1.0, 1), (1448, 48, 700.3, 1), (1000, 40, -1.0, 3)])
+@pytest.mark.parametrize("n,na,axis,slices", [(1448, 48, -1.0, 1), (1448, 48, 700.3, 1), (1000, 40, -1.0, 3),
+                                               (600, 12, -1.0, 1), (1448, 90, 731.6, 1), (2900, 90, -1.0, 1),
+                                               (2900, 37, 1420.25, 1)])
 def test_fp_with_few_tiles_splits_detectors(ufoir_lib, gpu_ctx, oracle, n, na, axis, slices):
     # few angles on few slices leave most SMs without an angle tile, so each
-    # tile's detectors are spread over several CTAs; results must not change
+    # tile's detectors are spread over several CTAs, each staging only the
+    # window of columns its rays reach; results must not change
     step = np.float32(np.pi / na)
     rng = np.random.default_rng(n + na + slices)
     vols = rng.random((slices, n, n), dtype=np.float32)

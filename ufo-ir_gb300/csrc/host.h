@@ -36,6 +36,7 @@ struct ufoir_projector {
     int n_tiles;
     int tiles_A;
     int tiles_valid;
+    float tiles_spread;         /* max over tiles of the angles' coordinate spread (columns) */
 };
 
 /* Scratch of the tiled forward projector: the padded copy and the padded

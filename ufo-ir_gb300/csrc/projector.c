@@ -278,6 +278,32 @@ int ufoir_projector_get_subsets(const ufoir_projector *proj, const ufoir_subset 
     return UFOIR_OK;
 }
 
+/* How far apart the rays of one detector at one row lie over the angles
+ * [first, first + count) of one direction, maximised over the image: the
+ * coordinate (…joseph.cl:68-75, 86) is linear in the detector and the row
+ * for each angle, so the spread is largest at the corners of the square.
+ * Evaluated in double; the kernel adds a margin for the float recurrence. */
+static double tile_spread(const ufoir_projector *p, unsigned int first, unsigned int count, int dir, double axis)
+{
+    const double n = (double) p->n_dets;
+    const double ros = (n - 2.0 * axis) / 2.0, os = n / 2.0;
+    double spread = 0.0;
+    for (int corner = 0; corner < 4; corner++) {
+        const double s = (corner & 1) ? n - 1.0 : 0.0, y = (corner & 2) ? n - 1.0 : 0.0;
+        double lo = 1e300, hi = -1e300;
+        for (unsigned int a = first; a < first + count; a++) {
+            const double sn = p->h_sin[a], cs = p->h_cos[a];
+            const double det_step = dir == UFOIR_HORIZONTAL ? -1.0 / sn : 1.0 / cs;
+            const double step = dir == UFOIR_HORIZONTAL ? cs / sn : sn / cs;
+            const double c = (0.5 + ros + s - 0.5 * n) * det_step - os * step + 0.5 * n + y * step;
+            lo = c < lo ? c : lo;
+            hi = c > hi ? c : hi;
+        }
+        spread = hi - lo > spread ? hi - lo : spread;
+    }
+    return spread;
+}
+
 /* Angle tiles of the tiled forward projector: runs of at most A angles that
  * never cross a direction boundary (the full subsets, cut into pieces). */
 static int ensure_tiles(ufoir_projector *p)
@@ -295,6 +321,9 @@ static int ensure_tiles(ufoir_projector *p)
     if (!h)
         return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
     int t = 0;
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    double spread = 0.0;
     for (unsigned int i = 0; i < p->n_subsets; i++)
         for (unsigned int a = 0; a < p->subsets[i].n; a += (unsigned int) A, t++) {
             const unsigned int left = p->subsets[i].n - a;
@@ -302,7 +331,11 @@ static int ensure_tiles(ufoir_projector *p)
             h[4 * t + 1] = (int) (left < (unsigned int) A ? left : (unsigned int) A);
             h[4 * t + 2] = p->subsets[i].direction;
             h[4 * t + 3] = 0;
+            const double sp = tile_spread(p, (unsigned int) h[4 * t + 0], (unsigned int) h[4 * t + 1],
+                                          p->subsets[i].direction, (double) g.axis);
+            spread = sp > spread ? sp : spread;
         }
+    p->tiles_spread = (float) spread;
     if (p->d_tiles)
         udev_free(ctx->dev, p->d_tiles);
     p->d_tiles = NULL;
@@ -359,8 +392,8 @@ int ufoir__fp_project(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol,
     ufoir__projector_geom(p, &g);
     const int rc = ensure_tiles(p);
     if (rc == UFOIR_OK)
-        return udev_fp_tiles(p->ctx->dev, &g, p->d_tiles, p->n_tiles, s->P, s->TP, src, w, w_shared, out, scale,
-                             n_slices);
+        return udev_fp_tiles(p->ctx->dev, &g, p->d_tiles, p->n_tiles, p->tiles_spread, s->P, s->TP, src, w, w_shared,
+                             out, scale, n_slices);
     if (rc != UFOIR_ERR_UNSUPPORTED)
         return rc;
     return udev_fp(p->ctx->dev, &g, 0, (int) p->n_angles, -1, vol, s->TP, src, w, w_shared, out, scale, n_slices);

@@ -14,7 +14,7 @@
 namespace tma {
 
 /* Error codes written to the kernel error word. */
-enum : int { kErrWaitTimeout = 1, kErrDrainTimeout = 2 };
+enum : int { kErrWaitTimeout = 1, kErrDrainTimeout = 2, kErrWindow = 8 };
 
 constexpr unsigned long long kWaitLimitNs = 250000000ull;   /* 250 ms */
 

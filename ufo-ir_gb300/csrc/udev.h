@@ -115,10 +115,13 @@ int udev_fp_tile_angles(udev *d, int n);
  * into buffers of n * pitch floats per slice whose pad columns are zero. */
 int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int n, int n_slices);
 /* Same contract as udev_fp over all angles, reading the padded images.
- * d_tiles: device array of int4 {first angle, count, direction, 0}. */
-int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, const float *volP,
-                  const float *volTP, const float *src, const float *w, int w_shared, float *out,
-                  float scale, int n_slices);
+ * d_tiles: device array of int4 {first angle, count, direction, 0};
+ * tile_spread: an upper bound, in columns, of how far the rays of one
+ * detector at one row lie apart over the angles of a tile (computed by the
+ * projector with its tiles), used to size the column windows of split tiles. */
+int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, float tile_spread,
+                  const float *volP, const float *volTP, const float *src, const float *w, int w_shared,
+                  float *out, float scale, int n_slices);
 /* Backprojection with shared-memory sinogram windows (udev_bp uses it for
  * 16 or more angles); same contract as udev_bp, at most 16 subsets. */
 int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
