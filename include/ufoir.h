@@ -119,7 +119,10 @@ typedef struct {
 
 /* Properties of the projector node, with the reference's names, ranges and
  * defaults (JSON keys in brackets):
- *   model            ["model"]            "joseph"      (…parallel-projector-task.c:123-128)
+ *   model            ["model"]            "joseph"      (…parallel-projector-task.c:123-128);
+ *                                         also "siddon": exact line integrals of the
+ *                                         pixel image and their adjoint (projector
+ *                                         calls only; the methods need "joseph")
  *   angles_num       ["angles_num"]       0 = from input dims[1] (:132-137, :315-317)
  *   is_forward       ["is_forward"]       1             (src/core/ufo-ir-state-dependent-task.c:75-80)
  *   axis_position    ["axis_position"]    -1 = n_dets/2 (src/core/ufo-ir-projector-task.c:68-73)
@@ -140,8 +143,10 @@ typedef struct ufoir_projector ufoir_projector;
 
 UFOIR_API void ufoir_projector_params_init(ufoir_projector_params *p);
 /* ufo_ir_parallel_projector_task_new (…parallel-projector-task.c:79-82) + setup (:360-388).
- * Fails with UFOIR_ERR_UNSUPPORTED unless model is "joseph" (case-insensitive,
- * the reference lower-cases it, :283-287). */
+ * Fails with UFOIR_ERR_UNSUPPORTED unless model is "joseph" or "siddon"
+ * (case-insensitive, the reference lower-cases it, :283-287). The methods
+ * (SART, SIRT, ASD-POCS, SBTV) fail with UFOIR_ERR_UNSUPPORTED on a
+ * "siddon" projector. */
 UFOIR_API int ufoir_projector_create(ufoir_ctx *ctx, const ufoir_projector_params *p,
                                      ufoir_projector **out);
 UFOIR_API void ufoir_projector_destroy(ufoir_projector *proj);

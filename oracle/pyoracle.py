@@ -148,6 +148,10 @@ def _declare(lib):
     lib.oracle_sart_d.argtypes = [pp, C.c_uint, C.c_float, f64p, f64p]
     lib.oracle_asdpocs_d.argtypes = [pp, C.POINTER(AsdpocsParams), f64p, f64p, f64p]
     lib.oracle_sbtv_d.argtypes = [pp, C.POINTER(SbtvParams), f64p, f64p]
+    lib.oracle_siddon_forward.argtypes = [C.c_uint, C.c_uint, f32p, f32p, C.c_float, f32p, f64p]
+    lib.oracle_siddon_backward.argtypes = [C.c_uint, C.c_uint, f32p, f32p, C.c_float, f32p, f64p]
+    lib.oracle_siddon_chord.argtypes = [C.c_uint, C.c_float, C.c_float, C.c_float, C.c_uint]
+    lib.oracle_siddon_chord.restype = C.c_double
     lib.oracle_set_threads.argtypes = [C.c_int]
     lib.oracle_get_threads.restype = C.c_int
 
@@ -329,3 +333,35 @@ def sbtv_d(p: Projector, sino, prm: SbtvParams):
     vol = np.zeros((p.n_dets, p.n_dets), np.float64)
     port_lib().oracle_sbtv_d(C.byref(p), C.byref(prm), _f64(s), _f64(vol))
     return vol
+
+
+# ---- the "siddon" model (siddon.c): double precision, pinned by the
+# analytic chord of a uniform image and by adjointness ----
+
+def _siddon_axis(n, axis):
+    return np.float32(0.5 * n) if axis < 0 else np.float32(axis)
+
+
+def siddon_forward(n, n_angles, step, vol, axis=-1.0):
+    s, c = lut(n_angles, np.float32(step))
+    sino = np.zeros((n_angles, n), np.float64)
+    port_lib().oracle_siddon_forward(n, n_angles, _f32(s), _f32(c), _siddon_axis(n, axis),
+                                     _f32(np.ascontiguousarray(vol, np.float32)), _f64(sino))
+    return sino
+
+
+def siddon_backward(n, n_angles, step, sino, axis=-1.0):
+    s, c = lut(n_angles, np.float32(step))
+    vol = np.zeros((n, n), np.float64)
+    port_lib().oracle_siddon_backward(n, n_angles, _f32(s), _f32(c), _siddon_axis(n, axis),
+                                      _f32(np.ascontiguousarray(sino, np.float32)), _f64(vol))
+    return vol
+
+
+def siddon_chords(n, n_angles, step, axis=-1.0):
+    """Projection of an image of ones: each ray's chord through the image square."""
+    s, c = lut(n_angles, np.float32(step))
+    ax = _siddon_axis(n, axis)
+    lib = port_lib()
+    return np.array([[lib.oracle_siddon_chord(n, s[a], c[a], ax, k) for k in range(n)]
+                     for a in range(n_angles)], np.float64)

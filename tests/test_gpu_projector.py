@@ -255,7 +255,7 @@ def test_work_queued_on_a_callers_stream(ufoir_lib, gpu_ctx, oracle):
 
 def test_errors_are_reported_not_fatal(ufoir_lib, gpu_ctx):
     with pytest.raises(ufoir_lib.UfoirError) as e:
-        ufoir_lib.ParallelProjector(gpu_ctx, model="siddon")
+        ufoir_lib.ParallelProjector(gpu_ctx, model="distance-driven")
     assert e.value.status == ufoir_lib.ERR_UNSUPPORTED
     with pytest.raises(ufoir_lib.UfoirError) as e:
         ufoir_lib.ParallelProjector(gpu_ctx, step=-1.0)
@@ -280,3 +280,75 @@ def test_sample_ceilings_are_measured(gpu_ctx):
     bp = gpu_ctx.sample_ceiling_bp()
     assert 1e11 < fp < 1e14 and 1e11 < bp < 1e14
     assert 0.5 < bp / fp < 2.0
+
+
+
+# ---- the "siddon" model: exact line integrals of the pixel image ----
+
+@pytest.mark.parametrize("n,na,axis,slices", [(64, 30, -1.0, 1), (100, 45, 47.3, 2), (367, 180, -1.0, 1),
+                                               (1448, 24, 731.6, 1)])
+def test_siddon_fp_bp_match_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, slices):
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(n * na + slices)
+    vols = rng.random((slices, n, n), dtype=np.float32)
+    sinos = rng.random((slices, na, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, axis, model="Siddon")
+    assert p.params.model == b"siddon"
+    got = p.forward(vols, np.zeros((slices, na, n), np.float32))
+    back = p.backward(np.zeros((slices, n, n), np.float32), sinos)
+    for i in range(slices):
+        assert rel_l2(got[i], oracle.siddon_forward(n, na, step, vols[i], axis)) <= TOL_ONE
+        assert rel_l2(back[i], oracle.siddon_backward(n, na, step, sinos[i], axis)) <= TOL_ONE
+    p.close()
+
+
+def test_siddon_projection_of_ones_is_the_chord(ufoir_lib, gpu_ctx, oracle):
+    n, na = 256, 37
+    step = np.float32(np.pi / na)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, 120.4, model="siddon")
+    got = p.forward(np.ones((n, n), np.float32), np.zeros((na, n), np.float32))
+    want = oracle.siddon_chords(n, na, step, 120.4)
+    assert np.abs(got - want).max() <= 1e-4 * n
+    assert rel_l2(got, want) <= TOL_ONE
+
+
+def test_siddon_backprojector_is_the_adjoint(ufoir_lib, gpu_ctx):
+    n, na = 200, 60
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(5)
+    x = rng.random((n, n), dtype=np.float32)
+    y = rng.random((na, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, model="siddon")
+    ax = p.forward(x, np.zeros((na, n), np.float32)).astype(np.float64)
+    aty = p.backward(np.zeros((n, n), np.float32), y).astype(np.float64)
+    lhs, rhs = float((ax * y).sum()), float((x * aty).sum())
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+
+
+def test_siddon_subsets_and_scale(ufoir_lib, gpu_ctx, oracle):
+    n, na = 80, 20
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(9)
+    vol = rng.random((n, n), dtype=np.float32)
+    sino0 = rng.random((na, n), dtype=np.float32)
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, model="siddon", correction_scale=-1.0, relaxation=0.5)
+    off, cnt, drn = (int(v) for v in p.subsets()[0])
+    got = p.subset_fp(vol, sino0.copy(), off, cnt, drn)
+    full = oracle.siddon_forward(n, na, step, vol)
+    want = sino0.astype(np.float64).copy()
+    rows = slice(off, off + cnt)
+    want[rows] = sino0[rows] - full[rows]
+    assert rel_l2(got, want) <= TOL_ONE
+    base = rng.random((n, n), dtype=np.float32)
+    only = np.zeros_like(sino0)
+    only[rows] = sino0[rows]
+    got_b = p.subset_bp(base.copy(), sino0, off, cnt, drn)
+    want_b = base + 0.5 * oracle.siddon_backward(n, na, step, only)
+    assert rel_l2(got_b, want_b) <= TOL_ONE
+
+
+def test_methods_need_the_joseph_model(ufoir_lib, gpu_ctx):
+    p = ufoir_lib.ParallelProjector(gpu_ctx, step=0.1, is_forward=0, model="siddon")
+    with pytest.raises(ufoir_lib.UfoirError) as e:
+        ufoir_lib.sirt(p, np.ones((10, 16), np.float32))
+    assert e.value.status == ufoir_lib.ERR_UNSUPPORTED and "Joseph" in str(e.value)

@@ -143,3 +143,27 @@ def test_fp_bp_adjointness_gap_is_measured_not_assumed(oracle):
     rhs = float(np.sum(x * aty))
     gap = abs(lhs - rhs) / abs(lhs)
     assert 0.05 < gap < 0.3
+
+
+# ---- the "siddon" model's oracle (no reference counterpart: pinned by an
+# analytic known answer and by adjointness) ----
+
+@pytest.mark.parametrize("n,na,axis", [(40, 13, -1.0), (40, 13, 17.3), (65, 7, 30.1), (16, 1, -1.0)])
+def test_kat_siddon_fp_of_ones_is_the_chord(oracle, n, na, axis):
+    # the projection of a uniform image is each ray's chord through the image square
+    step = np.float32(np.pi / na)
+    got = oracle.siddon_forward(n, na, step, np.ones((n, n), np.float32), axis)
+    want = oracle.siddon_chords(n, na, step, axis)
+    assert np.abs(got - want).max() < 1e-10
+
+
+@pytest.mark.parametrize("n,na,axis", [(40, 13, -1.0), (33, 9, 12.6)])
+def test_siddon_oracle_halves_are_adjoint(oracle, n, na, axis):
+    step = np.float32(np.pi / na)
+    rng = np.random.default_rng(n + na)
+    x = rng.random((n, n), dtype=np.float32)
+    y = rng.random((na, n), dtype=np.float32)
+    ax = oracle.siddon_forward(n, na, step, x, axis)
+    aty = oracle.siddon_backward(n, na, step, y, axis)
+    lhs, rhs = float((ax * y).sum()), float((x * aty).sum())
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)

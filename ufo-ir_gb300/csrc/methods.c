@@ -73,6 +73,9 @@ static int method_setup(ufoir_projector *proj, const size_t dims[2], size_t n_sl
         return ufoir__fail(ctx, UFOIR_ERR_INVALID,
                            "a method's projector must have is_forward = false (the method's output is the "
                            "projector's backward requisition)");
+    if (strcmp(proj->prm.model, "joseph") != 0)
+        return ufoir__fail(ctx, UFOIR_ERR_UNSUPPORTED,
+                           "the methods run the Joseph model only (projector model '%s')", proj->prm.model);
     int rc = ufoir__projector_prepare(proj, dims);
     if (rc)
         return rc;

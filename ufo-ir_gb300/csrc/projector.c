@@ -33,11 +33,13 @@ static int check_params(ufoir_ctx *ctx, ufoir_projector_params *p)
     for (i = 0; i + 1 < sizeof(lower) && p->model[i]; i++)
         lower[i] = (char) tolower((unsigned char) p->model[i]);
     lower[i] = 0;
-    /* set_model lower-cases the name (…parallel-projector-task.c:283-287);
-     * only projector-parallel-joseph.cl ships with the reference. */
-    if (strcmp(lower, "joseph") != 0)
-        return ufoir__fail(ctx, UFOIR_ERR_UNSUPPORTED, "projector model '%s' is not available (only 'joseph')",
-                           p->model);
+    /* set_model lower-cases the name (…parallel-projector-task.c:283-287).
+     * "joseph" is the reference's model (projector-parallel-joseph.cl);
+     * "siddon" adds exact line integrals of the pixel image (udev_siddon.cu),
+     * for the projector's own forward / backward / subset calls. */
+    if (strcmp(lower, "joseph") != 0 && strcmp(lower, "siddon") != 0)
+        return ufoir__fail(ctx, UFOIR_ERR_UNSUPPORTED,
+                           "projector model '%s' is not available ('joseph' or 'siddon')", p->model);
     memcpy(p->model, lower, sizeof(lower));
     /* GParamSpec ranges (ufo-ir-projector-task.c:68-93). */
     if (!(p->axis_position >= -1.0f))
@@ -408,10 +410,21 @@ int ufoir__fp_full(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, co
     return rc;
 }
 
+static int is_siddon(const ufoir_projector *p)
+{
+    return strcmp(p->prm.model, "siddon") == 0;
+}
+
 /* Forward projection of all angles of n_slices volumes (accumulating):
  * sino = sino + scale * A vol. */
 static int fp_all(ufoir_projector *p, const float *dvol, float *dsino, size_t n_slices)
 {
+    if (is_siddon(p)) {
+        udev_geom g;
+        ufoir__projector_geom(p, &g);
+        return udev_siddon_fp(p->ctx->dev, &g, 0, (int) p->n_angles, dvol, dsino, NULL, 0, dsino,
+                              p->prm.correction_scale, (int) n_slices);
+    }
     ufoir_fp_scratch s;
     int rc = ufoir__fp_scratch_alloc(p, &s, n_slices);
     if (rc)
@@ -425,6 +438,9 @@ static int bp_all(ufoir_projector *p, float *dvol, const float *dsino, size_t n_
 {
     udev_geom g;
     ufoir__projector_geom(p, &g);
+    if (is_siddon(p))
+        return udev_siddon_bp(p->ctx->dev, &g, p->subsets, (int) p->n_subsets, dsino, dvol, dvol,
+                              p->prm.relaxation, (int) n_slices);
     return udev_bp(p->ctx->dev, &g, p->subsets, (int) p->n_subsets, dsino, dvol, NULL, 0, NULL, dvol,
                    p->prm.relaxation, (int) n_slices);
 }
@@ -528,8 +544,12 @@ int ufoir_projector_subset_fp(ufoir_projector *proj, const float *vol, float *si
     UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns, 1));
     /* The subset's own direction picks the kernel (…parallel-projector-task.c:570). */
-    UFOIR_TRY(udev_fp(ctx->dev, &g, (int) s->offset, (int) s->n, s->direction ? 1 : 0, bv.dev, NULL, bs.dev,
-                      NULL, 0, bs.dev, proj->prm.correction_scale, 1));
+    if (is_siddon(proj))
+        UFOIR_TRY(udev_siddon_fp(ctx->dev, &g, (int) s->offset, (int) s->n, bv.dev, bs.dev, NULL, 0, bs.dev,
+                                 proj->prm.correction_scale, 1));
+    else
+        UFOIR_TRY(udev_fp(ctx->dev, &g, (int) s->offset, (int) s->n, s->direction ? 1 : 0, bv.dev, NULL, bs.dev,
+                          NULL, 0, bs.dev, proj->prm.correction_scale, 1));
     UFOIR_TRY(ufoir__buf_out(ctx, &bs, 1));
     UFOIR_TRY(udev_sync(ctx->dev));
 done:
@@ -554,7 +574,10 @@ int ufoir_projector_subset_bp(ufoir_projector *proj, float *vol, const float *si
     int rc;
     UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns, 1));
-    UFOIR_TRY(udev_bp(ctx->dev, &g, s, 1, bs.dev, bv.dev, NULL, 0, NULL, bv.dev, proj->prm.relaxation, 1));
+    if (is_siddon(proj))
+        UFOIR_TRY(udev_siddon_bp(ctx->dev, &g, s, 1, bs.dev, bv.dev, bv.dev, proj->prm.relaxation, 1));
+    else
+        UFOIR_TRY(udev_bp(ctx->dev, &g, s, 1, bs.dev, bv.dev, NULL, 0, NULL, bv.dev, proj->prm.relaxation, 1));
     UFOIR_TRY(ufoir__buf_out(ctx, &bv, 1));
     UFOIR_TRY(udev_sync(ctx->dev));
 done:

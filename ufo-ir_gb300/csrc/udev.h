@@ -132,6 +132,16 @@ int udev_memset(udev *d, void *p, int value, size_t bytes);
  * bounded-wait timeout since the last check; waits for the stream. */
 int udev_take_kernel_error(udev *d);
 
+/* The "siddon" model (udev_siddon.cu): exact line integrals of the pixel
+ * image, bin k of angle theta being the line X cos - Y sin + axis = k + 0.5.
+ * Forward over angles [a0, a0 + na): out = (src + scale * S) [* w] (src may
+ * be NULL or equal out); backward: for each subset v = v + relax * sum, with
+ * v starting from base (may alias dst) or 0; at most 16 subsets. */
+int udev_siddon_fp(udev *d, const udev_geom *g, int a0, int na, const float *vol, const float *src,
+                   const float *w, int w_shared, float *out, float scale, int n_slices);
+int udev_siddon_bp(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
+                   const float *sino, const float *base, float *dst, float relax, int n_slices);
+
 /* Pixel-driven backprojection over a list of subsets:
  *   v = base ? base : 0;  for each subset: v = v + relax * sum_{angles} lerp(sino)
  *   if cw: v = v * cw;  if add: v = v + add;  dst = v
