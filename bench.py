@@ -282,6 +282,7 @@ def run_ufoir(args, dist):
     if not args.quick and not args.no_serve and dist.rank == 0:
         serve = serve_section(ufoir, ctx)
     methods = methods_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
+    models = projector_models_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
 
     # roofline of the dominant kernel (live CUDA-event durations above)
     peak, peak_kind = measured_peaks()
@@ -339,6 +340,8 @@ def run_ufoir(args, dist):
         out["serve"] = serve
     if methods is not None:
         out["methods"] = methods
+    if models is not None:
+        out["projector_models"] = models
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and not args.quick:
         out["cpu_baseline"] = cpu_baseline(noisy[0])
     d_sino.close()
@@ -532,6 +535,36 @@ def methods_section(ufoir, ctx):
         proj.close()
         d_sino.close()
         d_vol.close()
+    return out
+
+
+def projector_models_section(ufoir, ctx, n=1448, na=1200, reps=5):
+    """Forward and backward projection of one resident slice (n^2 grid, na
+    angles) under each projector model: the mean time of one call over reps
+    calls, after one untimed call, and its rate in pixel-angle pairs per second."""
+    from ufoir import synth
+    step = float(np.float32(np.pi / na))
+    vol = synth.phantom_for(n, 1024, "ellipses", seed=9100)[None]
+    d_vol = ufoir.DeviceArray.from_numpy(ctx, vol.astype(np.float32))
+    d_sino = ufoir.DeviceArray(ctx, (1, na, n), zero=True)
+    out = {"workload": f"one slice, {n}^2 grid, {na} angles, {n} bins, resident in HBM"}
+    for model in ("joseph", "siddon"):
+        row = {}
+        for direction in ("forward", "backward"):
+            proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, model=model,
+                                           is_forward=1 if direction == "forward" else 0)
+            call = getattr(proj, direction)
+            call(d_vol, d_sino)
+            ctx.synchronize()
+            ctx.timer_begin()
+            for _ in range(reps):
+                call(d_vol, d_sino)
+            ms = ctx.timer_end() / reps
+            row[direction] = {"ms": ms, "pixel_angles_per_s": n * n * na / (ms * 1e-3)}
+            proj.close()
+        out[model] = row
+    d_vol.close()
+    d_sino.close()
     return out
 
 

@@ -78,17 +78,15 @@ __global__ void __launch_bounds__(128) siddon_fp_kernel(SiddonFpArgs P)
             const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
             const float c0f = floorf(lo);
             const int c0 = (int) c0f;
-            float v0 = (c0 >= 0 && c0 < n) ? __ldg(img + (size_t) j * n + c0) : 0.0f;
-            if (hi > c0f + 1.0f) {
-                /* crosses the boundary at column c0 + 1 */
-                const float f = (c0f + 1.0f - lo) / (hi - lo);
-                const float v1 = (c0 + 1 >= 0 && c0 + 1 < n) ? __ldg(img + (size_t) j * n + c0 + 1) : 0.0f;
-                sum += len * (f * v0 + (1.0f - f) * v1);
-            } else {
-                sum += len * v0;
-            }
+            const bool cross = hi > c0f + 1.0f;   /* crosses the boundary at column c0 + 1 */
+            const float v0 = (unsigned int) c0 < (unsigned int) n ? __ldg(img + (size_t) j * n + c0) : 0.0f;
+            const float v1 = cross && (unsigned int) (c0 + 1) < (unsigned int) n
+                                 ? __ldg(img + (size_t) j * n + c0 + 1) : 0.0f;
+            const float f = cross ? __fdividef(c0f + 1.0f - lo, hi - lo) : 1.0f;
+            sum += f * v0 + (1.0f - f) * v1;
             xa = xb;
         }
+        sum *= len;
     } else {
         /* columns: Y(X) = (X cos - u0) / sin, |dY/dX| < 1 */
         const float len = 1.0f / fabsf(sn);
@@ -100,16 +98,15 @@ __global__ void __launch_bounds__(128) siddon_fp_kernel(SiddonFpArgs P)
             const float lo = fminf(ya, yb), hi = fmaxf(ya, yb);
             const float r0f = floorf(lo);
             const int r0 = (int) r0f;
-            float v0 = (r0 >= 0 && r0 < n) ? __ldg(img + (size_t) r0 * n + i) : 0.0f;
-            if (hi > r0f + 1.0f) {
-                const float f = (r0f + 1.0f - lo) / (hi - lo);
-                const float v1 = (r0 + 1 >= 0 && r0 + 1 < n) ? __ldg(img + (size_t) (r0 + 1) * n + i) : 0.0f;
-                sum += len * (f * v0 + (1.0f - f) * v1);
-            } else {
-                sum += len * v0;
-            }
+            const bool cross = hi > r0f + 1.0f;
+            const float v0 = (unsigned int) r0 < (unsigned int) n ? __ldg(img + (size_t) r0 * n + i) : 0.0f;
+            const float v1 = cross && (unsigned int) (r0 + 1) < (unsigned int) n
+                                 ? __ldg(img + (size_t) (r0 + 1) * n + i) : 0.0f;
+            const float f = cross ? __fdividef(r0f + 1.0f - lo, hi - lo) : 1.0f;
+            sum += f * v0 + (1.0f - f) * v1;
             ya = yb;
         }
+        sum *= len;
     }
     const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + k;
     float result = P.src ? P.src[oidx] : 0.0f;
@@ -137,60 +134,101 @@ struct SiddonBpArgs {
     unsigned int sub_n[kMaxSub];
 };
 
-/* Grid (ceil(n / 32), ceil(n / 8), slices), block 32 x 8: thread = pixel. */
-__global__ void __launch_bounds__(256) siddon_bp_kernel(SiddonBpArgs P)
+/* Per angle, per block: the constants of L and the bin coordinate of the
+ * block's centre, C = Xc cos - Yc sin + axis - 0.5, split as kb + frac
+ * (kb an integer, frac a float). */
+struct SiddonAngle {
+    float4 geo;     /* cos, sin, frac, 1 / r */
+    float4 shape;   /* p, w, h = 1 / max(a, b), 1 / (a b) */
+    int kb;
+};
+
+constexpr int kBpW = 32, kBpH = 8, kBpThreads = kBpW * kBpH;
+
+/* Grid (ceil(n / 32), ceil(n / 8), slices), block 32 x 8: thread = pixel.
+ * The block's threads stage up to 256 angles' constants in shared memory,
+ * then each pixel visits the two bins whose lines can cross it: with
+ * t = uc - 0.5 the bin coordinate of its centre, bins floor(t) and
+ * floor(t) + 1 at distances frac(t) and 1 - frac(t) (every other bin is at
+ * least one bin away, beyond the support (a + b) / 2 <= 0.7072). */
+__global__ void __launch_bounds__(kBpThreads) siddon_bp_kernel(SiddonBpArgs P)
 {
-    const int i = (int) (blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = (int) (blockIdx.y * blockDim.y + threadIdx.y);
+    __shared__ SiddonAngle ang[kBpThreads];
+    const int tid = (int) (threadIdx.y * kBpW + threadIdx.x);
+    const int i = (int) (blockIdx.x * kBpW + threadIdx.x);
+    const int j = (int) (blockIdx.y * kBpH + threadIdx.y);
     const int slice = (int) blockIdx.z;
     const int n = P.n;
-    if (i >= n || j >= n)
-        return;
     const float half = 0.5f * (float) n;
-    const float X = ((float) i + 0.5f) - half, Y = ((float) j + 0.5f) - half;
+    /* block centre and the pixel's offset from it (both exact: half-integers) */
+    const float Xc = (float) (blockIdx.x * kBpW + kBpW / 2) - half;
+    const float Yc = (float) (blockIdx.y * kBpH + kBpH / 2) - half;
+    const float dx = ((float) threadIdx.x + 0.5f) - (float) (kBpW / 2);
+    const float dy = ((float) threadIdx.y + 0.5f) - (float) (kBpH / 2);
+    const bool inside = i < n && j < n;
     const float *sino = P.sino + (size_t) slice * P.sino_stride;
     const size_t pix = (size_t) slice * P.vol_stride + (size_t) j * n + i;
-    float v = P.base ? P.base[pix] : 0.0f;
+    float v = (inside && P.base) ? P.base[pix] : 0.0f;
     for (int s = 0; s < P.n_subsets; ++s) {
+        const int count = (int) P.sub_n[s];
         float sum = 0.0f;
-        for (unsigned int q = 0; q < P.sub_n[s]; ++q) {
-            const int angle = (int) (P.sub_offset[s] + q);
-            const float sr = __ldg(P.sinv + angle), cr = __ldg(P.cosv + angle);
-            const float r = sqrtf(sr * sr + cr * cr), ir = 1.0f / r;
-            const float a = fabsf(cr) * ir, b = fabsf(sr) * ir;
-            /* X cos - Y sin, kept as s + e with both products' rounding errors
-             * (exact by FMA) and the difference's (TwoSum), so that the small
-             * offset of a bin from the centre is computed without cancellation */
-            /* (explicit rounding: no contraction may merge these steps) */
-            const float pa = __fmul_rn(X, cr), pb = __fmul_rn(Y, sr);
-            const float ea = fmaf(X, cr, -pa), eb = fmaf(Y, sr, -pb);
-            const float s = __fsub_rn(pa, pb);
-            const float bv = __fsub_rn(s, pa);
-            const float es = __fadd_rn(__fsub_rn(pa, __fsub_rn(s, bv)), __fsub_rn(-pb, bv));
-            const float e = __fadd_rn(es, __fsub_rn(ea, eb));
-            const float uc = s + P.axis;                    /* bin coordinate of the centre (bounds only) */
-            const float w = 0.5f * (a + b), p = 0.5f * fabsf(a - b);
-            const float h = 1.0f / fmaxf(a, b);
-            const float ab = a * b;
-            /* bins k with |k + 0.5 - uc| / r < w: at most two */
-            const int k0 = max(0, (int) ceilf(uc - w * r - 0.5f));
-            const int k1 = min(n - 1, (int) floorf(uc + w * r - 0.5f));
-            const float *row = sino + (size_t) angle * n;
-            for (int k = k0; k <= k1; ++k) {
-                const float dd = fabsf(__fsub_rn(__fsub_rn(__fsub_rn((float) k + 0.5f, P.axis), s), e)) * ir;
-                float L;
-                if (dd <= p)
-                    L = h;
-                else if (dd < w)
-                    L = (w - dd) / ab;
-                else
-                    L = 0.0f;
-                sum += L * __ldg(row + k);
+        for (int q0 = 0; q0 < count; q0 += kBpThreads) {
+            const int nq = min(kBpThreads, count - q0);
+            if (tid < nq) {
+                const int angle = (int) P.sub_offset[s] + q0 + tid;
+                const float cr = __ldg(P.cosv + angle), sr = __ldg(P.sinv + angle);
+                const float r = sqrtf(cr * cr + sr * sr), ir = 1.0f / r;
+                const float a = fabsf(cr) * ir, b = fabsf(sr) * ir;
+                const float ab = a * b;
+                /* Xc cos - Yc sin + (axis - 0.5) as hi + lo: the products'
+                 * rounding errors (exact by FMA) and both sums' (TwoSum), with
+                 * explicit rounding so that no contraction merges the steps */
+                const float pa = __fmul_rn(Xc, cr), pb = __fmul_rn(Yc, sr);
+                const float ea = fmaf(Xc, cr, -pa), eb = fmaf(Yc, sr, -pb);
+                const float s1 = __fsub_rn(pa, pb);
+                const float b1 = __fsub_rn(s1, pa);
+                const float e1 = __fadd_rn(__fsub_rn(pa, __fsub_rn(s1, b1)), __fsub_rn(-pb, b1));
+                const float ax = P.axis - 0.5f;
+                const float hi = __fadd_rn(s1, ax);
+                const float b2 = __fsub_rn(hi, s1);
+                const float e2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(hi, b2)), __fsub_rn(ax, b2));
+                const float kbf = floorf(hi);
+                SiddonAngle A;
+                /* hi - kb is exact (the fraction bits of hi) */
+                const float frac = __fadd_rn(__fsub_rn(hi, kbf), __fadd_rn(__fadd_rn(e1, __fsub_rn(ea, eb)), e2));
+                A.geo = make_float4(cr, sr, frac, ir);
+                A.shape = make_float4(0.5f * fabsf(a - b), 0.5f * (a + b), 1.0f / fmaxf(a, b),
+                                      ab > 0.0f ? 1.0f / ab : 3.0e38f);
+                A.kb = (int) kbf;
+                ang[tid] = A;
             }
+            __syncthreads();
+            if (inside) {
+                const float *row = sino + (size_t) (P.sub_offset[s] + q0) * n;
+#pragma unroll 4
+                for (int q = 0; q < nq; ++q, row += n) {
+                    const float4 g = ang[q].geo;
+                    const float4 h = ang[q].shape;
+                    const int kb = ang[q].kb;
+                    const float t = g.z + fmaf(dx, g.x, -(dy * g.y));
+                    const float m = floorf(t);
+                    const float f = t - m;                 /* exact */
+                    const int ka = kb + (int) m;
+                    const float da = f * g.w, db = (1.0f - f) * g.w;
+                    const float la = da <= h.x ? h.z : fmaxf(0.0f, (h.y - da) * h.w);
+                    const float lb = db <= h.x ? h.z : fmaxf(0.0f, (h.y - db) * h.w);
+                    const float va = (unsigned int) ka < (unsigned int) n ? __ldg(row + ka) : 0.0f;
+                    const float vb = (unsigned int) (ka + 1) < (unsigned int) n ? __ldg(row + ka + 1) : 0.0f;
+                    sum = fmaf(la, va, sum);
+                    sum = fmaf(lb, vb, sum);
+                }
+            }
+            __syncthreads();
         }
         v += P.relax * sum;
     }
-    P.dst[pix] = v;
+    if (inside)
+        P.dst[pix] = v;
 }
 
 }  // namespace
@@ -259,7 +297,7 @@ extern "C" int udev_siddon_bp(udev *d, const udev_geom *g, const ufoir_subset *s
     A.relax = relax;
     A.vol_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
-    dim3 grid(udev_div_up(n, 32), udev_div_up(n, 8), (unsigned int) n_slices);
-    siddon_bp_kernel<<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    dim3 grid(udev_div_up(n, kBpW), udev_div_up(n, kBpH), (unsigned int) n_slices);
+    siddon_bp_kernel<<<grid, dim3(kBpW, kBpH), 0, d->stream>>>(A);
     return udev_after_launch(d, "siddon_bp_kernel");
 }
