@@ -44,10 +44,22 @@ def test_sirt_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, sli
     assert p.params.relaxation == np.float32(0.25) and p.params.correction_scale == -1.0
 
 
+def _kernels(monkeypatch, kernels):
+    """SART's kernels: "auto" (the padded per-angle kernels where they serve
+    the geometry, else the general ones) or "general" (always the general
+    per-angle kernels)."""
+    if kernels == "auto":
+        monkeypatch.delenv("UFOIR_SART_KERNELS", raising=False)
+    else:
+        monkeypatch.setenv("UFOIR_SART_KERNELS", kernels)
+
+
+@pytest.mark.parametrize("kernels", ["auto", "general"])
 @pytest.mark.parametrize("n,na,axis,iters,slices", [(16, 12, -1.0, 2, 1), (33, 40, 15.3, 2, 2),
                                                      (48, 36, -1.0, 1, 1), (100, 60, -1.0, 1, 2),
                                                      (130, 50, 64.7, 2, 1)])
-def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
+def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, monkeypatch, kernels, n, na, axis, iters, slices):
+    _kernels(monkeypatch, kernels)
     rng = np.random.default_rng(3 * n + na)
     step = np.float32(np.pi / na)
     sinos = rng.random((slices, na, n), dtype=np.float32) * n
@@ -64,11 +76,13 @@ def test_sart_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, sli
 # sums), with a launch shape per size: 16-row segments (n <= 1024), one block
 # per warp (1111, 1448, 2900), several blocks per warp (2900 x 2 slices,
 # 4100); off-centre axes give inactive detectors and clamped tiles.
-@pytest.mark.parametrize("n,na,axis,iters,slices", [(513, 24, -1.0, 1, 1), (600, 40, 290.6, 2, 2),
-                                                     (1111, 30, -1.0, 1, 1), (1448, 36, 700.25, 1, 1),
-                                                     (2900, 12, -1.0, 1, 1), (2900, 6, 1449.5, 1, 2),
-                                                     (4100, 6, -1.0, 1, 1)])
-def test_sart_chunked_sizes_match_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):
+@pytest.mark.parametrize("kernels,n,na,axis,iters,slices", [
+    ("auto", 513, 24, -1.0, 1, 1), ("auto", 600, 40, 290.6, 2, 2), ("general", 600, 40, 290.6, 2, 2),
+    ("auto", 1111, 30, -1.0, 1, 1), ("auto", 1448, 36, 700.25, 1, 1), ("auto", 2900, 12, -1.0, 1, 1),
+    ("auto", 2900, 6, 1449.5, 1, 2), ("auto", 4100, 6, -1.0, 1, 1)])
+def test_sart_chunked_sizes_match_oracle(ufoir_lib, gpu_ctx, oracle, monkeypatch, kernels, n, na, axis, iters,
+                                         slices):
+    _kernels(monkeypatch, kernels)
     rng = np.random.default_rng(5 * n + na)
     step = np.float32(np.pi / na)
     sinos = rng.random((slices, na, n), dtype=np.float32) * n
@@ -92,7 +106,9 @@ def test_sart_crossed_clamp_edges_match_oracle(ufoir_lib, gpu_ctx, oracle, axis)
     assert np.array_equal(got, want), np.abs(got - want).max()
 
 
-def test_asdpocs_chunked_size_matches_oracle(ufoir_lib, gpu_ctx, oracle):
+@pytest.mark.parametrize("kernels", ["auto", "general"])
+def test_asdpocs_chunked_size_matches_oracle(ufoir_lib, gpu_ctx, oracle, monkeypatch, kernels):
+    _kernels(monkeypatch, kernels)
     n, na = 530, 24
     step = np.float32(np.pi / na)
     vol = np.random.default_rng(23).random((n, n), dtype=np.float32)
@@ -202,8 +218,10 @@ def test_norms_match_oracle(ufoir_lib, gpu_ctx, oracle):
         assert abs(gpu_ctx.dot_product(a, b) - d64) <= 1e-6 * (abs(d64) + 1)
 
 
-def test_c1_sart_full_size(ufoir_lib, gpu_ctx, oracle):
+@pytest.mark.parametrize("kernels", ["auto", "general"])
+def test_c1_sart_full_size(ufoir_lib, gpu_ctx, oracle, monkeypatch, kernels):
     # SART on the 367-bin, 180-angle geometry with a 256^2 phantom (2 iterations).
+    _kernels(monkeypatch, kernels)
     from ufoir import synth
     n, na = 367, 180
     step = np.float32(np.pi / na)

@@ -384,8 +384,12 @@ int ufoir__sart_body(void *arg)
     /* sart-task.c:209-217: per angle, r_theta = (b_theta - A_theta x) * R_theta;
      * x = x + lambda A_theta^T r_theta. The volume lives in the layout of the
      * current direction run, transposed while the angles are horizontal, so
-     * that every ray walks rows. */
-    if (udev_sart_padded(d, &s->g, S)) {
+     * that every ray walks rows.
+     * The padded kernels where they serve the geometry, else the general
+     * ones; UFOIR_SART_KERNELS=general selects the general kernels always. */
+    const char *only = getenv("UFOIR_SART_KERNELS");
+    const int general_only = only && strcmp(only, "general") == 0;
+    if (!general_only && udev_sart_padded(d, &s->g, S)) {
         /* padded copies V (vertical run) and H (horizontal run) in s->work */
         int place = -1;
         for (unsigned int a = 0; a < s->p->n_angles && rc == UFOIR_OK; a++) {
