@@ -99,28 +99,27 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, 1) fp_tiles_kernel
      * adjacent angles through adjacent detectors meet a row within ~25
      * words, so a warp's shared loads stay free of bank conflicts, which 32
      * adjacent detectors of one angle (spread 1/|cos| apart) are not.
-     * A thread owns A/2 angles x 2J detectors d0 + i * half; detectors
-     * (2m, 2m + 1) of one angle travel as a pair through packed FP32. */
+     * A thread owns A/2 angles x 2J detectors d0 + 16 i, so a warp's rays
+     * are 32J adjacent detectors of A adjacent angles, which cross the
+     * image together (see the chunk modes below); detectors (2m, 2m + 1) of
+     * one angle travel as a pair through packed FP32. Slots past the tile's
+     * angles or the CTA's detectors repeat its last angle or detector (their
+     * sums are not written), so every slot holds a ray of the image. */
     constexpr int A2 = A / 2;
     const int lane = (int) (threadIdx.x & 31);
     const int g = lane >> 4;
-    const int half = (int) (blockDim.x >> 1);
-    const int d0 = dstart + (int) (threadIdx.x >> 5) * 16 + (lane & 15);
+    const int d0 = dstart + (int) (threadIdx.x >> 5) * 32 * J + (lane & 15);
     float2 c[A2][J], inner[A2][J], sum[A2][J], stp[A2];
 #pragma unroll
     for (int k = 0; k < A2; ++k) {
-        const int a = g + 2 * k;
-        float st = 0.0f, det_step = 0.0f;
-        if (a < tile.y) {
-            const int angle = tile.x + a;
-            joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, st);
-        }
+        const int angle = tile.x + min(g + 2 * k, tile.y - 1);
+        float st, det_step;
+        joseph::ray_steps(dir, __ldg(P.sinv + angle), __ldg(P.cosv + angle), det_step, st);
         stp[k] = joseph::splat(st);
 #pragma unroll
         for (int m = 0; m < J; ++m) {
-            const int s0 = d0 + 2 * m * half, s1 = s0 + half;
-            c[k][m] = make_float2((a < tile.y && s0 < dend) ? joseph::ray_start(kc, s0, n, det_step, st) : 0.0f,
-                                  (a < tile.y && s1 < dend) ? joseph::ray_start(kc, s1, n, det_step, st) : 0.0f);
+            const int s0 = min(d0 + 32 * m, dend - 1), s1 = min(d0 + 32 * m + 16, dend - 1);
+            c[k][m] = make_float2(joseph::ray_start(kc, s0, n, det_step, st), joseph::ray_start(kc, s1, n, det_step, st));
             inner[k][m] = make_float2(0.0f, 0.0f);
             sum[k][m] = make_float2(0.0f, 0.0f);
         }
@@ -195,7 +194,20 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, 1) fp_tiles_kernel
 
     /* A tap pair starts at padded column floor(c - 0.5) + kPadL; pairs that
      * start outside [0, n + 2] lie wholly in the zero border, so the start
-     * is clamped (as unsigned) to n + 2, whose taps are two pad zeros. */
+     * is clamped (as unsigned) to n + 2, whose taps are two pad zeros.
+     * Each warp picks one of three forms per chunk, from its rays'
+     * coordinates at the chunk's first and last rows (monotone along a ray;
+     * the float recurrence drifts < 0.03 columns over a chunk, and the
+     * bounds keep 0.25):
+     *  - inside: every coordinate lies in [0.5, n + 1.5) and in the staged
+     *    columns, so floor(c - 0.5) takes the three-operation form
+     *    (floor_half2) and the tap address is one multiply-add on its bits,
+     *    with no clamp;
+     *  - outside: every coordinate is below -0.5 or at least n + 0.5, where
+     *    both taps are border zeros. Only the recurrence advances: adding
+     *    +-0 leaves a block sum unchanged (it starts at +0 and a sum of
+     *    finite floats in round-to-nearest is never -0);
+     *  - otherwise the general form above. */
     const uint32_t col_lim = (uint32_t) n + 2u;
     const float2 z2 = joseph::splat(P.neg_zero);
     const uint32_t stage_s = (uint32_t) __cvta_generic_to_shared(stage0);
@@ -210,35 +222,87 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, 1) fp_tiles_kernel
         const int r0 = ch * K;
         const int rows = min(K, n - r0);
         if (ok) {
-            uint32_t row_s = stage_s + 4u * (uint32_t) (st * (int) stage_floats);
+            const uint32_t row_s0 = stage_s + 4u * (uint32_t) (st * (int) stage_floats);
             /* padded column - window start, clamped (as unsigned) to the zero taps */
-            const int colbits = WIN ? kColBits + w0s[st] : kColBits;
+            const int w0 = WIN ? w0s[st] : 0;
+            const int colbits = kColBits + w0;
             const uint32_t lim = WIN ? (uint32_t) wcols : col_lim;
-            for (int r = 0; r < rows; ++r, row_s += 4u * (uint32_t) wstride) {
+            /* the chunk's form */
+            const float span = (float) (rows - 1);
+            const float in_lo = fmaxf(0.5f, (float) (w0 - kPadL) + 0.5f) + 0.25f;
+            const float in_hi = (float) ((int) lim - kPadL + w0) + 1.25f;
+            const float out_hi = (float) n + 0.75f;
+            bool inside = true, outside = true;
 #pragma unroll
-                for (int k = 0; k < A2; ++k) {
+            for (int k = 0; k < A2; ++k)
 #pragma unroll
-                    for (int m = 0; m < J; ++m) {
-                        float2 t;
-                        const float2 y = joseph::floor_any2(c[k][m], t);
-                        const uint32_t p0 = min((uint32_t) (__float_as_int(y.x) - colbits), lim);
-                        const uint32_t p1 = min((uint32_t) (__float_as_int(y.y) - colbits), lim);
-                        const uint32_t a0 = row_s + 4u * p0, a1 = row_s + 4u * p1;
-                        const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
-                        const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
-                        inner[k][m] = joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
-                        c[k][m] = joseph::add2(c[k][m], stp[k]);
+                for (int m = 0; m < J; ++m) {
+                    const float ex = fmaf(span, stp[k].x, c[k][m].x), ey = fmaf(span, stp[k].y, c[k][m].y);
+                    const float lo = fminf(fminf(c[k][m].x, ex), fminf(c[k][m].y, ey));
+                    const float hi = fmaxf(fmaxf(c[k][m].x, ex), fmaxf(c[k][m].y, ey));
+                    inside = inside && lo >= in_lo && hi < in_hi;
+                    const bool xo = fmaxf(c[k][m].x, ex) < -0.75f || fminf(c[k][m].x, ex) >= out_hi;
+                    const bool yo = fmaxf(c[k][m].y, ey) < -0.75f || fminf(c[k][m].y, ey) >= out_hi;
+                    outside = outside && xo && yo;
+                }
+            inside = __all_sync(0xffffffffu, inside);
+            outside = !inside && __all_sync(0xffffffffu, outside);
+            if (inside) {
+                /* address = row + 4 (floor(c - 0.5) + kPadL - w0) = base + 4 bits(y) */
+                uint32_t base = row_s0 + 4u * (uint32_t) (kPadL - w0) - 4u * (uint32_t) joseph::kHalfFloorBits;
+                for (int r = 0; r < rows; ++r, base += 4u * (uint32_t) wstride) {
+#pragma unroll
+                    for (int k = 0; k < A2; ++k) {
+#pragma unroll
+                        for (int m = 0; m < J; ++m) {
+                            float2 t;
+                            const float2 y = joseph::floor_half2(c[k][m], t);
+                            const uint32_t a0 = base + 4u * (uint32_t) __float_as_int(y.x);
+                            const uint32_t a1 = base + 4u * (uint32_t) __float_as_int(y.y);
+                            const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
+                            const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
+                            inner[k][m] = joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
+                            c[k][m] = joseph::add2(c[k][m], stp[k]);
+                        }
                     }
                 }
-                if (((r0 + r + 1) & 63) == 0) {
+            } else if (outside) {
+                for (int r = 0; r < rows; ++r) {
 #pragma unroll
                     for (int k = 0; k < A2; ++k)
 #pragma unroll
-                        for (int m = 0; m < J; ++m) {
-                            sum[k][m] = joseph::add2(sum[k][m], inner[k][m]);
-                            inner[k][m] = make_float2(0.0f, 0.0f);
-                        }
+                        for (int m = 0; m < J; ++m)
+                            c[k][m] = joseph::add2(c[k][m], stp[k]);
                 }
+            } else {
+                uint32_t row_s = row_s0;
+                for (int r = 0; r < rows; ++r, row_s += 4u * (uint32_t) wstride) {
+#pragma unroll
+                    for (int k = 0; k < A2; ++k) {
+#pragma unroll
+                        for (int m = 0; m < J; ++m) {
+                            float2 t;
+                            const float2 y = joseph::floor_any2(c[k][m], t);
+                            const uint32_t p0 = min((uint32_t) (__float_as_int(y.x) - colbits), lim);
+                            const uint32_t p1 = min((uint32_t) (__float_as_int(y.y) - colbits), lim);
+                            const uint32_t a0 = row_s + 4u * p0, a1 = row_s + 4u * p1;
+                            const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
+                            const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
+                            inner[k][m] = joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
+                            c[k][m] = joseph::add2(c[k][m], stp[k]);
+                        }
+                    }
+                }
+            }
+            /* K divides 64: a 64-row block ends only at a chunk's last row */
+            if (((r0 + rows) & 63) == 0) {
+#pragma unroll
+                for (int k = 0; k < A2; ++k)
+#pragma unroll
+                    for (int m = 0; m < J; ++m) {
+                        sum[k][m] = joseph::add2(sum[k][m], inner[k][m]);
+                        inner[k][m] = make_float2(0.0f, 0.0f);
+                    }
             }
         }
         ok = __syncthreads_and(ok) != 0;
@@ -272,7 +336,7 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, 1) fp_tiles_kernel
         const int angle = tile.x + a;
 #pragma unroll
         for (int i = 0; i < 2 * J; ++i) {
-            const int s = d0 + i * half;
+            const int s = d0 + i * 16;
             if (s >= dend)
                 continue;
             const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + s;
