@@ -314,7 +314,11 @@ def run_ufoir(args, dist):
                    "bp_frac_of_fp_ceiling": bp_rate / ceiling if ceiling else None,
                    "ceiling": "measured in this run: each projector's exact per-sample sequence from "
                               "shared memory on every SM, no global traffic (ufoir_sample_ceiling for the "
-                              "FP, ufoir_sample_ceiling_bp for the BP)"}
+                              "FP, ufoir_sample_ceiling_bp for the BP)",
+                   "fp_samples_note": "the FP's samples are every sample of the reference's 64-sample blocks; "
+                                      "where all rays of a warp lie outside the image for a chunk of rows (about "
+                                      "an eighth of the chunks at this geometry) the samples are border zeros "
+                                      "and only the coordinate recurrence runs, so fp_frac can pass 1"}
     dom_rate = fp_rate if dom == "fp" else bp_rate
     dom_ceiling = ceiling if dom == "fp" else ceiling_bp
     roofline["compute_bound"] = {
