@@ -417,19 +417,30 @@ static int is_siddon(const ufoir_projector *p)
 
 /* Forward projection of all angles of n_slices volumes (accumulating):
  * sino = sino + scale * A vol. */
+/* Siddon forward projection of angles [a0, a0 + na): the padded copies
+ * first (scratch s), then the ray walk. */
+static int siddon_fp(ufoir_projector *p, ufoir_fp_scratch *s, int a0, int na, const float *dvol, float *dsino,
+                     int n_slices)
+{
+    udev_geom g;
+    ufoir__projector_geom(p, &g);
+    int rc = udev_pad_transpose(p->ctx->dev, dvol, s->P, s->TP, (int) p->n_dets, n_slices);
+    if (!rc)
+        rc = udev_siddon_fp(p->ctx->dev, &g, a0, na, s->P, s->TP, dsino, NULL, 0, dsino, p->prm.correction_scale,
+                            n_slices);
+    return rc;
+}
+
 static int fp_all(ufoir_projector *p, const float *dvol, float *dsino, size_t n_slices)
 {
-    if (is_siddon(p)) {
-        udev_geom g;
-        ufoir__projector_geom(p, &g);
-        return udev_siddon_fp(p->ctx->dev, &g, 0, (int) p->n_angles, dvol, dsino, NULL, 0, dsino,
-                              p->prm.correction_scale, (int) n_slices);
-    }
     ufoir_fp_scratch s;
     int rc = ufoir__fp_scratch_alloc(p, &s, n_slices);
     if (rc)
         return rc;
-    rc = ufoir__fp_full(p, &s, dvol, dsino, NULL, 0, dsino, p->prm.correction_scale, (int) n_slices);
+    if (is_siddon(p))
+        rc = siddon_fp(p, &s, 0, (int) p->n_angles, dvol, dsino, (int) n_slices);
+    else
+        rc = ufoir__fp_full(p, &s, dvol, dsino, NULL, 0, dsino, p->prm.correction_scale, (int) n_slices);
     ufoir__fp_scratch_free(p, &s);
     return rc;
 }
@@ -544,10 +555,14 @@ int ufoir_projector_subset_fp(ufoir_projector *proj, const float *vol, float *si
     UFOIR_TRY(ufoir__buf_in(ctx, &bv, vol, nv, 1));
     UFOIR_TRY(ufoir__buf_in(ctx, &bs, sino, ns, 1));
     /* The subset's own direction picks the kernel (…parallel-projector-task.c:570). */
-    if (is_siddon(proj))
-        UFOIR_TRY(udev_siddon_fp(ctx->dev, &g, (int) s->offset, (int) s->n, bv.dev, bs.dev, NULL, 0, bs.dev,
-                                 proj->prm.correction_scale, 1));
-    else
+    if (is_siddon(proj)) {
+        ufoir_fp_scratch fs;
+        UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &fs, 1));
+        rc = siddon_fp(proj, &fs, (int) s->offset, (int) s->n, bv.dev, bs.dev, 1);
+        ufoir__fp_scratch_free(proj, &fs);
+        if (rc)
+            goto done;
+    } else
         UFOIR_TRY(udev_fp(ctx->dev, &g, (int) s->offset, (int) s->n, s->direction ? 1 : 0, bv.dev, NULL, bs.dev,
                           NULL, 0, bs.dev, proj->prm.correction_scale, 1));
     UFOIR_TRY(ufoir__buf_out(ctx, &bs, 1));

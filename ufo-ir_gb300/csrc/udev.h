@@ -135,10 +135,12 @@ int udev_take_kernel_error(udev *d);
 /* The "siddon" model (udev_siddon.cu): exact line integrals of the pixel
  * image, bin k of angle theta being the line X cos - Y sin + axis = k + 0.5.
  * Forward over angles [a0, a0 + na): out = (src + scale * S) [* w] (src may
- * be NULL or equal out); backward: for each subset v = v + relax * sum, with
- * v starting from base (may alias dst) or 0; at most 16 subsets. */
-int udev_siddon_fp(udev *d, const udev_geom *g, int a0, int na, const float *vol, const float *src,
-                   const float *w, int w_shared, float *out, float scale, int n_slices);
+ * be NULL or equal out), reading the padded copy and padded transpose of
+ * udev_pad_transpose (n <= 32768); backward: for each subset
+ * v = v + relax * sum, with v starting from base (may alias dst) or 0; at
+ * most 16 subsets. */
+int udev_siddon_fp(udev *d, const udev_geom *g, int a0, int na, const float *volP, const float *volTP,
+                   const float *src, const float *w, int w_shared, float *out, float scale, int n_slices);
 int udev_siddon_bp(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
                    const float *sino, const float *base, float *dst, float relax, int n_slices);
 

@@ -17,9 +17,10 @@
  *   L(d) = ((a + b) / 2 - |d|) / (a b)   up to |d| = (a + b) / 2, 0 beyond.
  *
  * Forward: one thread per ray walks the slabs (rows for |cos| >= |sin|,
- * columns otherwise); in a slab the ray covers at most two pixels, and its
- * length in the slab (1 / max(a, b)) splits where it crosses the pixel
- * boundary. Backward: one thread per pixel evaluates L for the (at most
+ * columns otherwise) of the zero-padded image or its padded transpose, the
+ * copies the Joseph forward projector reads; in a slab the ray covers at
+ * most two pixels, and its length in the slab (1 / max(a, b)) splits where
+ * it crosses the pixel boundary. Backward: one thread per pixel evaluates L for the (at most
  * two) bins whose lines cross the pixel, per angle. Both compute the same
  * chord lengths, so the backprojector is the adjoint of the forward one up
  * to rounding. Arithmetic is FP32; the sums are per ray in slab order and
@@ -33,7 +34,8 @@
 namespace {
 
 struct SiddonFpArgs {
-    const float *vol;
+    const float *volP;      /* padded image rows (walked by row-mode rays) */
+    const float *volTP;     /* padded transposed rows (column-mode rays) */
     const float *src;
     const float *w;
     float *out;
@@ -42,14 +44,32 @@ struct SiddonFpArgs {
     int n;
     int a0;
     int na;
+    int pitch;
     float axis;
     float scale;
-    long long vol_stride;
+    long long volp_stride;
     long long sino_stride;
     long long w_stride;
 };
 
-/* Grid (ceil(n / 128), na, slices), 128 threads: thread = detector bin. */
+constexpr int kPadL = 2;                       /* zero columns left of a padded row */
+constexpr float kFloorMagic = 12582912.0f;     /* 1.5 * 2^23 */
+constexpr int kFloorMagicBits = 0x4B400000;
+
+/*
+ * Grid (ceil(n / 128), na, slices), 128 threads: thread = detector bin.
+ * A ray walks the rows of the padded image (rows for |cos| >= |sin|, else
+ * the rows of the padded transpose, i.e. the image's columns) with the
+ * coordinate across the slab at its lower edge, x0 + j slope, formed by one
+ * fma from the ray start (no drift). In slab j the ray spans [lo, hi]
+ * (hi - lo = |slope| <= 1): pixel floor(lo), and where it crosses the next
+ * boundary the fraction f = (floor(lo) + 1 - lo) / |slope| of the length
+ * stays in that pixel and 1 - f goes to the next. floor() is a
+ * round-toward-minus-infinity add of 1.5 * 2^23 (exact for |x| < 2^22);
+ * the padded column floor(lo) + 2 is clamped (as unsigned) to n + 2, whose
+ * two taps are pad zeros, so rays outside the image read zeros without
+ * bounds checks.
+ */
 __global__ void __launch_bounds__(128) siddon_fp_kernel(SiddonFpArgs P)
 {
     const int k = (int) (blockIdx.x * blockDim.x + threadIdx.x);
@@ -63,51 +83,32 @@ __global__ void __launch_bounds__(128) siddon_fp_kernel(SiddonFpArgs P)
     const float sn = sr / r, cs = cr / r;
     const float half = 0.5f * (float) n;
     const float u0 = (((float) k + 0.5f) - P.axis) / r;   /* X cos - Y sin = u0, unit normal */
-    const float *img = P.vol + (size_t) slice * P.vol_stride;
-    float sum = 0.0f;
-    if (fabsf(cs) >= fabsf(sn)) {
-        /* rows: X(Y) = (u0 + Y sin) / cos, |dX/dY| <= 1 */
-        const float len = 1.0f / fabsf(cs);
-        const float slope = sn / cs;
-        /* column coordinate at row j's lower edge, x0 + j slope with one
-         * rounding (no drift along the ray) */
-        const float x0 = u0 / cs + (-half) * slope + half;
-        float xa = x0;
-        for (int j = 0; j < n; ++j) {
-            const float xb = fmaf((float) (j + 1), slope, x0);
-            const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
-            const float c0f = floorf(lo);
-            const int c0 = (int) c0f;
-            const bool cross = hi > c0f + 1.0f;   /* crosses the boundary at column c0 + 1 */
-            const float v0 = (unsigned int) c0 < (unsigned int) n ? __ldg(img + (size_t) j * n + c0) : 0.0f;
-            const float v1 = cross && (unsigned int) (c0 + 1) < (unsigned int) n
-                                 ? __ldg(img + (size_t) j * n + c0 + 1) : 0.0f;
-            const float f = cross ? __fdividef(c0f + 1.0f - lo, hi - lo) : 1.0f;
-            sum += f * v0 + (1.0f - f) * v1;
-            xa = xb;
-        }
-        sum *= len;
-    } else {
-        /* columns: Y(X) = (X cos - u0) / sin, |dY/dX| < 1 */
-        const float len = 1.0f / fabsf(sn);
-        const float slope = cs / sn;
-        const float y0 = (-u0) / sn + (-half) * slope + half;   /* row coordinate at column i's left edge */
-        float ya = y0;
-        for (int i = 0; i < n; ++i) {
-            const float yb = fmaf((float) (i + 1), slope, y0);
-            const float lo = fminf(ya, yb), hi = fmaxf(ya, yb);
-            const float r0f = floorf(lo);
-            const int r0 = (int) r0f;
-            const bool cross = hi > r0f + 1.0f;
-            const float v0 = (unsigned int) r0 < (unsigned int) n ? __ldg(img + (size_t) r0 * n + i) : 0.0f;
-            const float v1 = cross && (unsigned int) (r0 + 1) < (unsigned int) n
-                                 ? __ldg(img + (size_t) (r0 + 1) * n + i) : 0.0f;
-            const float f = cross ? __fdividef(r0f + 1.0f - lo, hi - lo) : 1.0f;
-            sum += f * v0 + (1.0f - f) * v1;
-            ya = yb;
-        }
-        sum *= len;
+    const bool rows = fabsf(cs) >= fabsf(sn);
+    /* rows: X(Y) = (u0 + Y sin) / cos; columns: Y(X) = (X cos - u0) / sin */
+    const float len = rows ? 1.0f / fabsf(cs) : 1.0f / fabsf(sn);
+    const float slope = rows ? sn / cs : cs / sn;
+    const float x0 = (rows ? u0 / cs : (-u0) / sn) + (-half) * slope + half;
+    const float inv = 1.0f / fabsf(slope);         /* inf for slope 0: never crosses */
+    const float *img = (rows ? P.volP : P.volTP) + (size_t) slice * P.volp_stride;
+    const uint32_t lim = (uint32_t) n + 2u;
+    float sum = 0.0f, xa = x0, jf = 0.0f;
+    uint32_t ro = 0;
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) {
+        jf += 1.0f;
+        const float xb = fmaf(jf, slope, x0);
+        const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
+        const float y = __fadd_rd(lo, kFloorMagic);
+        const float c1 = (y - kFloorMagic) + 1.0f;        /* floor(lo) + 1 */
+        const uint32_t p = min((uint32_t) (__float_as_int(y) - (kFloorMagicBits - kPadL)), lim);
+        const float *row = img + ro + p;
+        const float v0 = __ldg(row), v1 = __ldg(row + 1);
+        const float f = hi > c1 ? fminf((c1 - lo) * inv, 1.0f) : 1.0f;
+        sum += f * v0 + (1.0f - f) * v1;
+        xa = xb;
+        ro += (uint32_t) P.pitch;
     }
+    sum *= len;
     const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + k;
     float result = P.src ? P.src[oidx] : 0.0f;
     result += P.scale * sum;
@@ -233,20 +234,21 @@ __global__ void __launch_bounds__(kBpThreads) siddon_bp_kernel(SiddonBpArgs P)
 
 }  // namespace
 
-extern "C" int udev_siddon_fp(udev *d, const udev_geom *g, int a0, int na, const float *vol, const float *src,
-                              const float *w, int w_shared, float *out, float scale, int n_slices)
+extern "C" int udev_siddon_fp(udev *d, const udev_geom *g, int a0, int na, const float *volP, const float *volTP,
+                              const float *src, const float *w, int w_shared, float *out, float scale, int n_slices)
 {
     if (n_slices <= 0 || na <= 0)
         return UFOIR_OK;
     const int n = g->n_dets;
-    if (a0 < 0 || a0 + na > g->n_angles || n < 1 || n_slices > 65535 || na > 65535) {
-        udev_set_error(d, "siddon_fp: angles [%d, %d) of %d, %d slices out of range", a0, a0 + na, g->n_angles,
-                       n_slices);
+    if (a0 < 0 || a0 + na > g->n_angles || n < 1 || n > 32768 || n_slices > 65535 || na > 65535) {
+        udev_set_error(d, "siddon_fp: angles [%d, %d) of %d, n = %d, %d slices out of range", a0, a0 + na,
+                       g->n_angles, n, n_slices);
         return UFOIR_ERR_INVALID;
     }
     UDEV_BIND(d);
     SiddonFpArgs A;
-    A.vol = vol;
+    A.volP = volP;
+    A.volTP = volTP;
     A.src = src;
     A.w = w;
     A.out = out;
@@ -255,9 +257,10 @@ extern "C" int udev_siddon_fp(udev *d, const udev_geom *g, int a0, int na, const
     A.n = n;
     A.a0 = a0;
     A.na = na;
+    A.pitch = udev_fp_pitch(n);
     A.axis = g->axis;
     A.scale = scale;
-    A.vol_stride = (long long) n * n;
+    A.volp_stride = (long long) n * A.pitch;
     A.sino_stride = (long long) g->n_angles * n;
     A.w_stride = w_shared ? 0 : A.sino_stride;
     dim3 grid(udev_div_up(n, 128), (unsigned int) na, (unsigned int) n_slices);
