@@ -145,34 +145,51 @@ struct SiddonAngle {
 };
 
 constexpr int kBpW = 32, kBpH = 8, kBpThreads = kBpW * kBpH;
+constexpr int kBpPx = 2;                       /* pixels per thread, 32 columns apart */
+constexpr int kBpTileW = kBpW * kBpPx;         /* tile: 64 x 8 pixels */
 
-/* Grid (ceil(n / 32), ceil(n / 8), slices), block 32 x 8: thread = pixel.
+/* Grid (ceil(n / 64), ceil(n / 8), slices), block 32 x 8: a thread owns
+ * pixels tx and tx + 32 of its tile row.
  * The block's threads stage up to 256 angles' constants in shared memory,
  * then each pixel visits the two bins whose lines can cross it: with
  * t = uc - 0.5 the bin coordinate of its centre, bins floor(t) and
  * floor(t) + 1 at distances frac(t) and 1 - frac(t) (every other bin is at
- * least one bin away, beyond the support (a + b) / 2 <= 0.7072). */
+ * least one bin away, beyond the support (a + b) / 2 <= 0.7072). A pixel's
+ * t is the tile centre's fraction plus its offset (|dx| <= 31.5, |dy| <= 3.5)
+ * times cos and sin, two fmas: ~2e-6 bins of rounding. */
 __global__ void __launch_bounds__(kBpThreads) siddon_bp_kernel(SiddonBpArgs P)
 {
     __shared__ SiddonAngle ang[kBpThreads];
     const int tid = (int) (threadIdx.y * kBpW + threadIdx.x);
-    const int i = (int) (blockIdx.x * kBpW + threadIdx.x);
+    const int i0 = (int) (blockIdx.x * kBpTileW + threadIdx.x);
     const int j = (int) (blockIdx.y * kBpH + threadIdx.y);
     const int slice = (int) blockIdx.z;
     const int n = P.n;
     const float half = 0.5f * (float) n;
-    /* block centre and the pixel's offset from it (both exact: half-integers) */
-    const float Xc = (float) (blockIdx.x * kBpW + kBpW / 2) - half;
+    /* tile centre and the pixels' offsets from it (all exact: half-integers) */
+    const float Xc = (float) (blockIdx.x * kBpTileW + kBpTileW / 2) - half;
     const float Yc = (float) (blockIdx.y * kBpH + kBpH / 2) - half;
-    const float dx = ((float) threadIdx.x + 0.5f) - (float) (kBpW / 2);
+    float dx[kBpPx];
+    bool inside[kBpPx];
+    size_t pix[kBpPx];
+    float v[kBpPx];
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < kBpPx; ++u) {
+        dx[u] = ((float) (threadIdx.x + kBpW * u) + 0.5f) - (float) (kBpTileW / 2);
+        inside[u] = i0 + kBpW * u < n && j < n;
+        any = any || inside[u];
+        pix[u] = (size_t) slice * P.vol_stride + (size_t) j * n + (size_t) (i0 + kBpW * u);
+        v[u] = (inside[u] && P.base) ? P.base[pix[u]] : 0.0f;
+    }
     const float dy = ((float) threadIdx.y + 0.5f) - (float) (kBpH / 2);
-    const bool inside = i < n && j < n;
     const float *sino = P.sino + (size_t) slice * P.sino_stride;
-    const size_t pix = (size_t) slice * P.vol_stride + (size_t) j * n + i;
-    float v = (inside && P.base) ? P.base[pix] : 0.0f;
     for (int s = 0; s < P.n_subsets; ++s) {
         const int count = (int) P.sub_n[s];
-        float sum = 0.0f;
+        float sum[kBpPx];
+#pragma unroll
+        for (int u = 0; u < kBpPx; ++u)
+            sum[u] = 0.0f;
         for (int q0 = 0; q0 < count; q0 += kBpThreads) {
             const int nq = min(kBpThreads, count - q0);
             if (tid < nq) {
@@ -204,32 +221,40 @@ __global__ void __launch_bounds__(kBpThreads) siddon_bp_kernel(SiddonBpArgs P)
                 ang[tid] = A;
             }
             __syncthreads();
-            if (inside) {
+            if (any) {
                 const float *row = sino + (size_t) (P.sub_offset[s] + q0) * n;
-#pragma unroll 4
+#pragma unroll 2
                 for (int q = 0; q < nq; ++q, row += n) {
                     const float4 g = ang[q].geo;
                     const float4 h = ang[q].shape;
                     const int kb = ang[q].kb;
-                    const float t = g.z + fmaf(dx, g.x, -(dy * g.y));
-                    const float m = floorf(t);
-                    const float f = t - m;                 /* exact */
-                    const int ka = kb + (int) m;
-                    const float da = f * g.w, db = (1.0f - f) * g.w;
-                    const float la = da <= h.x ? h.z : fmaxf(0.0f, (h.y - da) * h.w);
-                    const float lb = db <= h.x ? h.z : fmaxf(0.0f, (h.y - db) * h.w);
-                    const float va = (unsigned int) ka < (unsigned int) n ? __ldg(row + ka) : 0.0f;
-                    const float vb = (unsigned int) (ka + 1) < (unsigned int) n ? __ldg(row + ka + 1) : 0.0f;
-                    sum = fmaf(la, va, sum);
-                    sum = fmaf(lb, vb, sum);
+                    const float ty = fmaf(-dy, g.y, g.z);
+#pragma unroll
+                    for (int u = 0; u < kBpPx; ++u) {
+                        const float t = fmaf(dx[u], g.x, ty);
+                        const float m = floorf(t);
+                        const float f = t - m;                 /* exact */
+                        const int ka = kb + (int) m;
+                        const float da = f * g.w, db = g.w - da;
+                        const float la = da <= h.x ? h.z : fmaxf(0.0f, (h.y - da) * h.w);
+                        const float lb = db <= h.x ? h.z : fmaxf(0.0f, (h.y - db) * h.w);
+                        const float va = (unsigned int) ka < (unsigned int) n ? __ldg(row + ka) : 0.0f;
+                        const float vb = (unsigned int) (ka + 1) < (unsigned int) n ? __ldg(row + ka + 1) : 0.0f;
+                        sum[u] = fmaf(la, va, sum[u]);
+                        sum[u] = fmaf(lb, vb, sum[u]);
+                    }
                 }
             }
             __syncthreads();
         }
-        v += P.relax * sum;
+#pragma unroll
+        for (int u = 0; u < kBpPx; ++u)
+            v[u] += P.relax * sum[u];
     }
-    if (inside)
-        P.dst[pix] = v;
+#pragma unroll
+    for (int u = 0; u < kBpPx; ++u)
+        if (inside[u])
+            P.dst[pix[u]] = v[u];
 }
 
 }  // namespace
@@ -300,7 +325,7 @@ extern "C" int udev_siddon_bp(udev *d, const udev_geom *g, const ufoir_subset *s
     A.relax = relax;
     A.vol_stride = (long long) n * n;
     A.sino_stride = (long long) g->n_angles * n;
-    dim3 grid(udev_div_up(n, kBpW), udev_div_up(n, kBpH), (unsigned int) n_slices);
+    dim3 grid(udev_div_up(n, kBpTileW), udev_div_up(n, kBpH), (unsigned int) n_slices);
     siddon_bp_kernel<<<grid, dim3(kBpW, kBpH), 0, d->stream>>>(A);
     return udev_after_launch(d, "siddon_bp_kernel");
 }
