@@ -585,7 +585,15 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serve trace")
     ap.add_argument("--methods", action="store_true",
                     help="also time one call of each other configured method workload (C1, C2, C3a/b, C4)")
+    ap.add_argument("--projector-models", action="store_true",
+                    help="only time the Joseph and Siddon projectors on one resident 1448^2 x 1200 slice")
     args = ap.parse_args()
+    if args.projector_models:
+        import ufoir
+        ctx = ufoir.Context(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(projector_models_section(ufoir, ctx)), flush=True)
+        ctx.close()
+        return
     dist = Dist()
     try:
         out = run_reference(args, dist) if args.impl == "reference" else run_ufoir(args, dist)
