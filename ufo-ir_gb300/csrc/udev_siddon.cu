@@ -70,6 +70,33 @@ constexpr int kFloorMagicBits = 0x4B400000;
  * two taps are pad zeros, so rays outside the image read zeros without
  * bounds checks.
  */
+template <bool UP>
+__device__ __forceinline__ float siddon_walk(const float *__restrict__ img, int n, int pitch, float x0, float slope,
+                                             float inv)
+{
+    const uint32_t lim = (uint32_t) n + 2u;
+    float sum = 0.0f, xa = x0, jf = 0.0f;
+    uint32_t ro = 0;
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) {
+        jf += 1.0f;
+        const float xb = fmaf(jf, slope, x0);
+        const float lo = UP ? xa : xb;
+        const float y = __fadd_rd(lo, kFloorMagic);
+        const float c1 = (y - kFloorMagic) + 1.0f;        /* floor(lo) + 1 */
+        const uint32_t p = min((uint32_t) (__float_as_int(y) - (kFloorMagicBits - kPadL)), lim);
+        const float *row = img + ro + p;
+        const float v0 = __ldg(row), v1 = __ldg(row + 1);
+        /* the part of the slab's length left of the boundary c1: all of it
+         * when the ray does not reach c1 ((c1 - lo) / |slope| >= 1) */
+        const float f = fminf((c1 - lo) * inv, 1.0f);
+        sum += f * v0 + (1.0f - f) * v1;
+        xa = xb;
+        ro += (uint32_t) pitch;
+    }
+    return sum;
+}
+
 __global__ void __launch_bounds__(128) siddon_fp_kernel(SiddonFpArgs P)
 {
     const int k = (int) (blockIdx.x * blockDim.x + threadIdx.x);
@@ -90,28 +117,13 @@ __global__ void __launch_bounds__(128) siddon_fp_kernel(SiddonFpArgs P)
     const float x0 = (rows ? u0 / cs : (-u0) / sn) + (-half) * slope + half;
     const float inv = 1.0f / fabsf(slope);         /* inf for slope 0: never crosses */
     const float *img = (rows ? P.volP : P.volTP) + (size_t) slice * P.volp_stride;
-    const uint32_t lim = (uint32_t) n + 2u;
-    float sum = 0.0f, xa = x0, jf = 0.0f;
-    uint32_t ro = 0;
-#pragma unroll 4
-    for (int j = 0; j < n; ++j) {
-        jf += 1.0f;
-        const float xb = fmaf(jf, slope, x0);
-        const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
-        const float y = __fadd_rd(lo, kFloorMagic);
-        const float c1 = (y - kFloorMagic) + 1.0f;        /* floor(lo) + 1 */
-        const uint32_t p = min((uint32_t) (__float_as_int(y) - (kFloorMagicBits - kPadL)), lim);
-        const float *row = img + ro + p;
-        const float v0 = __ldg(row), v1 = __ldg(row + 1);
-        const float f = hi > c1 ? fminf((c1 - lo) * inv, 1.0f) : 1.0f;
-        sum += f * v0 + (1.0f - f) * v1;
-        xa = xb;
-        ro += (uint32_t) P.pitch;
-    }
-    sum *= len;
+    /* the slope's sign is the angle's (uniform per block), so each loop
+     * knows which slab end is the lower one */
+    const float sum = slope >= 0.0f ? siddon_walk<true>(img, n, P.pitch, x0, slope, inv)
+                                    : siddon_walk<false>(img, n, P.pitch, x0, slope, inv);
     const size_t oidx = (size_t) slice * P.sino_stride + (size_t) angle * n + k;
     float result = P.src ? P.src[oidx] : 0.0f;
-    result += P.scale * sum;
+    result += P.scale * (sum * len);
     if (P.w)
         result *= P.w[(size_t) slice * P.w_stride + (size_t) angle * n + k];
     P.out[oidx] = result;
