@@ -152,7 +152,7 @@ struct SiddonBpArgs {
  * (kb an integer, frac a float). */
 struct SiddonAngle {
     float4 geo;     /* cos, sin, frac, 1 / r */
-    float4 shape;   /* p, w, h = 1 / max(a, b), 1 / (a b) */
+    float4 shape;   /* p, w / (a b), h = 1 / max(a, b), 1 / (a b) */
     int kb;
 };
 
@@ -227,8 +227,10 @@ __global__ void __launch_bounds__(kBpThreads) siddon_bp_kernel(SiddonBpArgs P)
                 /* hi - kb is exact (the fraction bits of hi) */
                 const float frac = __fadd_rn(__fsub_rn(hi, kbf), __fadd_rn(__fadd_rn(e1, __fsub_rn(ea, eb)), e2));
                 A.geo = make_float4(cr, sr, frac, ir);
-                A.shape = make_float4(0.5f * fabsf(a - b), 0.5f * (a + b), 1.0f / fmaxf(a, b),
-                                      ab > 0.0f ? 1.0f / ab : 3.0e38f);
+                /* 1 / (a b) stays finite (3e38) for axis-aligned angles, where
+                 * every offset beyond p = w gets L = 0 */
+                const float iab = ab > 0.0f ? 1.0f / ab : 3.0e38f;
+                A.shape = make_float4(0.5f * fabsf(a - b), 0.5f * (a + b) * iab, 1.0f / fmaxf(a, b), iab);
                 A.kb = (int) kbf;
                 ang[tid] = A;
             }
@@ -244,12 +246,14 @@ __global__ void __launch_bounds__(kBpThreads) siddon_bp_kernel(SiddonBpArgs P)
 #pragma unroll
                     for (int u = 0; u < kBpPx; ++u) {
                         const float t = fmaf(dx[u], g.x, ty);
-                        const float m = floorf(t);
-                        const float f = t - m;                 /* exact */
-                        const int ka = kb + (int) m;
+                        /* floor(t) by a round-down add of 1.5 * 2^23 (|t| < 2^22) */
+                        const float y = __fadd_rd(t, kFloorMagic);
+                        const float f = t - (y - kFloorMagic);     /* exact */
+                        const int ka = kb + (__float_as_int(y) - kFloorMagicBits);
                         const float da = f * g.w, db = g.w - da;
-                        const float la = da <= h.x ? h.z : fmaxf(0.0f, (h.y - da) * h.w);
-                        const float lb = db <= h.x ? h.z : fmaxf(0.0f, (h.y - db) * h.w);
+                        /* L(d) = h up to p, then (w - d) / (a b) down to 0 */
+                        const float la = da <= h.x ? h.z : fmaxf(0.0f, fmaf(-da, h.w, h.y));
+                        const float lb = db <= h.x ? h.z : fmaxf(0.0f, fmaf(-db, h.w, h.y));
                         const float va = (unsigned int) ka < (unsigned int) n ? __ldg(row + ka) : 0.0f;
                         const float vb = (unsigned int) (ka + 1) < (unsigned int) n ? __ldg(row + ka + 1) : 0.0f;
                         sum[u] = fmaf(la, va, sum[u]);
