@@ -312,13 +312,15 @@ def test_siddon_projection_of_ones_is_the_chord(ufoir_lib, gpu_ctx, oracle):
     assert rel_l2(got, want) <= TOL_ONE
 
 
-def test_siddon_backprojector_is_the_adjoint(ufoir_lib, gpu_ctx):
-    n, na = 200, 60
+# <A x, y> = <x, A^T y>: a property of any size, here also the full
+# 1448^2 x 1200 geometry with an off-centre axis.
+@pytest.mark.parametrize("n,na,axis", [(200, 60, -1.0), (1448, 1200, 731.6)])
+def test_siddon_backprojector_is_the_adjoint(ufoir_lib, gpu_ctx, n, na, axis):
     step = np.float32(np.pi / na)
     rng = np.random.default_rng(5)
     x = rng.random((n, n), dtype=np.float32)
     y = rng.random((na, n), dtype=np.float32)
-    p = _proj(ufoir_lib, gpu_ctx, n, na, step, model="siddon")
+    p = _proj(ufoir_lib, gpu_ctx, n, na, step, axis, model="siddon")
     ax = p.forward(x, np.zeros((na, n), np.float32)).astype(np.float64)
     aty = p.backward(np.zeros((n, n), np.float32), y).astype(np.float64)
     lhs, rhs = float((ax * y).sum()), float((x * aty).sum())
