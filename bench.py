@@ -482,8 +482,11 @@ METHOD_CASES = (
 )
 
 
-# methods whose whole call the oracle port runs in seconds on the host cores
-METHOD_CPU = ("sart", "asdpocs")
+# methods whose call on one slice the oracle port runs on the host cores: SART
+# and ASD-POCS in seconds, 10 SIRT iterations at 1448^2 x 1200 in about 15 s,
+# one SBTV outer iteration at 1448^2 x 720 (about 60 FP + BP applications) in
+# about a minute
+METHOD_CPU = ("sart", "sirt", "asdpocs", "sbtv")
 
 
 def method_cpu_baseline(method, n, na, step, sino, kw):
@@ -500,6 +503,11 @@ def method_cpu_baseline(method, n, na, step, sino, kw):
     t0 = time.perf_counter()
     if method == "sart":
         pyoracle.sart(p, sino, kw["num_iterations"], 0.25)
+    elif method == "sirt":
+        pyoracle.sirt(p, sino, kw["num_iterations"], 0.25)
+    elif method == "sbtv":
+        pyoracle.sbtv(p, sino, pyoracle.sbtv_params(num_iterations=kw["num_iterations"], lambda_=kw["lambda"],
+                                                    mu=kw["mu"], norm_mode=pyoracle.NORM_FP64))
     else:
         pyoracle.asdpocs(p, sino, pyoracle.asdpocs_params(num_iterations=kw["num_iterations"],
                                                          norm_mode=pyoracle.NORM_FP64))
