@@ -69,8 +69,12 @@ struct FpTileArgs {
 
 constexpr int kMaxWinThreads = 448;   /* detector-split CTAs hold at most half the slots */
 
+/* Windowed CTAs of the J = 1 variants made for large n (A <= 4) hold few
+ * rays per thread: two of them per SM. (The A = 8 variant, the default at
+ * n <= 768, measured 4 % slower held to that register budget.) */
 template <int J, int A, bool WIN>
-__global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, 1) fp_tiles_kernel(FpTileArgs P)
+__global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && A <= 4) ? 2 : 1)
+    fp_tiles_kernel(FpTileArgs P)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
@@ -459,6 +463,10 @@ int udev_kernels_init(udev *d)
                                        d->smem_optin));
     UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<8, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        d->smem_optin));
+    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       d->smem_optin));
+    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       d->smem_optin));
     return UFOIR_OK;
 }
 
@@ -521,7 +529,7 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
      * max |det_step| = sqrt 2, the chunk's rows times max |step| = 1, the
      * spread of the tile's angles, and a margin), unless that is the whole
      * row. */
-    int threads = cfg.threads, K = cfg.K;
+    int threads = cfg.threads, K = cfg.K, win_j = cfg.J;
     A.dsplit = 1;
     A.dper = n;
     A.wcols = A.pitch;
@@ -542,6 +550,12 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
             const int slots = (A.dper + 2 * cfg.J - 1) / (2 * cfg.J);
             threads = (slots + 15) / 16 * 32;
             K = k2;
+            /* Windowed CTAs take one detector pair per angle slot (J = 1)
+             * where that fits: a split CTA holds few rays, and at J = 4
+             * (n = 2900) it would run 3 warps of 16 rays per thread, too few
+             * warps to hide the loads. */
+            const int slots1 = (A.dper + 1) / 2, threads1 = (slots1 + 15) / 16 * 32;
+            const int threads_win = threads1 <= kMaxWinThreads ? threads1 : threads;
             /* the column window, with the largest chunk that keeps two CTAs per SM */
             for (int kw = 32; kw >= 4; kw /= 2) {
                 const double need = (double) (A.dper - 1) * 1.41422 + (double) (kw - 1) + (double) tile_spread +
@@ -549,11 +563,14 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
                 const int wc = ((int) ceil(need) + 3) / 4 * 4;
                 if (wc >= A.pitch)
                     break;
-                if (threads <= kMaxWinThreads &&
+                if (threads_win <= kMaxWinThreads &&
                     2 * (kHeader + 2 * (size_t) kw * (wc + 4) * 4) <= (size_t) d->smem_optin) {
                     A.wcols = wc;
                     A.wstride = wc + 4;
                     K = kw;
+                    if (threads_win == threads1)
+                        win_j = 1;
+                    threads = threads_win;
                     break;
                 }
             }
@@ -562,7 +579,9 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
     A.rows_per_chunk = K;
     const size_t smem = kHeader + 2 * (size_t) K * A.wstride * 4;
     if (A.wcols < A.pitch) {
-        switch (cfg.J * 16 + cfg.A) {
+        switch (win_j * 16 + cfg.A) {
+        case 1 * 16 + 4: return launch_tiles<1, 4, true>(d, A, n_tiles, n_slices, threads, smem);
+        case 1 * 16 + 2: return launch_tiles<1, 2, true>(d, A, n_tiles, n_slices, threads, smem);
         case 1 * 16 + 8: return launch_tiles<1, 8, true>(d, A, n_tiles, n_slices, threads, smem);
         case 2 * 16 + 8: return launch_tiles<2, 8, true>(d, A, n_tiles, n_slices, threads, smem);
         case 4 * 16 + 4: return launch_tiles<4, 4, true>(d, A, n_tiles, n_slices, threads, smem);
