@@ -285,8 +285,11 @@ def test_sample_ceilings_are_measured(gpu_ctx):
 
 # ---- the "siddon" model: exact line integrals of the pixel image ----
 
-@pytest.mark.parametrize("n,na,axis,slices", [(64, 30, -1.0, 1), (100, 45, 47.3, 2), (367, 180, -1.0, 1),
-                                               (1448, 24, 731.6, 1)])
+# Tiny and odd sizes (rays mostly at the image border), 4 angles (one at
+# exactly 45 degrees, where the walk direction is decided by the float LUT),
+# off-centre axes, several slices, and the full C2 width.
+@pytest.mark.parametrize("n,na,axis,slices", [(5, 3, -1.0, 1), (7, 4, 2.2, 3), (64, 30, -1.0, 1),
+                                               (100, 45, 47.3, 2), (367, 180, -1.0, 1), (1448, 24, 731.6, 1)])
 def test_siddon_fp_bp_match_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, slices):
     step = np.float32(np.pi / na)
     rng = np.random.default_rng(n * na + slices)
