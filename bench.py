@@ -19,6 +19,11 @@ relaxation_factor 0.25.
           oracle port of its kernels and host loop, all host threads).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ufoir|reference]
+                       [--methods] [--quick] [--no-serve] [--projector-models]
+  --methods            also time the other method workloads (C1, C2 one slice,
+                       C3a/b, C4) with a CPU oracle baseline each, and the
+                       Joseph/Siddon projector pair
+  --projector-models   only the Joseph/Siddon projector timing on one slice
 """
 import argparse
 import json
