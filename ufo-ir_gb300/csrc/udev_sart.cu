@@ -318,6 +318,19 @@ struct SartFpArgs {
 constexpr int kFpCluster = 8;                       /* CTAs per ray group at most (portable cluster) */
 constexpr int kFpLocal = kMaxBlocks / kFpCluster;   /* blocks per CTA at most */
 
+/* Programmatic dependent launch: let the next kernel in the stream launch
+ * now, and wait here until the previous one has completed and its writes are
+ * visible (both return at once when the launch did not allow overlap). */
+__device__ __forceinline__ void pdl_launch_next()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+__device__ __forceinline__ void pdl_wait_previous()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ void cluster_sync_all()
 {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
@@ -404,6 +417,7 @@ __global__ void __launch_bounds__(32 * W, MINB) sart_fp_kernel(SartFpArgs P)
     const int slice = (int) blockIdx.z;
     const int n = P.n, nb = P.n_blocks;
     const int s0 = g * 64 + lane, s1 = s0 + 32;
+    pdl_launch_next();
 
     /* CTA 0 fetches its rays' src and w early */
     const int sr = g * 64 + (int) threadIdx.x;
@@ -422,6 +436,8 @@ __global__ void __launch_bounds__(32 * W, MINB) sart_fp_kernel(SartFpArgs P)
     const float hi = (float) (n + 1);
     const float *tab = P.table + (size_t) P.angle * nb * n;
     const float *img0 = P.img + (size_t) slice * P.img_stride + kSartPadL - joseph::kFloorMagicBits;
+    /* the volume was written by the previous kernel */
+    pdl_wait_previous();
 
     if (SEG == 4) {
         for (int i = 0; rank + C * i < nb; ++i) {
@@ -576,6 +592,7 @@ template <bool T, int ROWS>
 __global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
 {
     __shared__ __align__(16) float rs[kBpSpan];
+    pdl_launch_next();
     const int n = P.n;
     const int lane = (int) threadIdx.x;
     const int i_base = (int) blockIdx.x * kBpTileW, j_base = (int) blockIdx.y * (8 * ROWS);
@@ -600,6 +617,8 @@ __global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
             atomicOr(P.err, kErrSpan);
         return;
     }
+    /* the residual row and the volume were written by earlier kernels */
+    pdl_wait_previous();
     /* the tile's pixels first: their loads overlap the staging below */
     const int i0 = i_base + lane;
     bool okc[4];
@@ -840,6 +859,18 @@ static SartFpShape sart_fp_shape(udev *d, int n, int n_slices)
     return f;
 }
 
+/* Overlap each per-angle kernel's launch and geometry prologue with the end
+ * of the previous one (programmatic dependent launch) when both kernels'
+ * grids fit on the GPU together: then a waiting CTA takes no SM another
+ * one needs (with larger grids that overlap was measured slower). */
+static bool sart_pdl(udev *d, int n, int n_slices)
+{
+    const SartFpShape f = sart_fp_shape(d, n, n_slices);
+    const long long fp_ctas = (long long) ((n + 63) / 64) * f.cluster * n_slices;
+    const long long bp_ctas = (long long) udev_div_up(n, kBpTileW) * udev_div_up(n, 32) * n_slices;
+    return fp_ctas + bp_ctas <= udev_sm_count(d);
+}
+
 extern "C" int udev_sart_padded(udev *d, const udev_geom *g, int n_slices)
 {
     if (!sart_geometry_ok(g) || n_slices < 1 || n_slices > 65535)
@@ -937,13 +968,18 @@ extern "C" int udev_sart_fp(udev *d, const udev_geom *g, int angle, int dir, con
     cfg.gridDim = dim3((unsigned int) (groups * A.cluster), 1, (unsigned int) n_slices);
     cfg.blockDim = dim3((unsigned int) f.threads, 1, 1);
     cfg.stream = d->stream;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned int) A.cluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    if (sart_pdl(d, n, n_slices)) {
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.numAttrs = 2;
+    }
     cudaError_t e = f.shape == 0   ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<4, 16, 4, 3>, A)
                     : f.shape == 1 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 16, 4, 3>, A)
                     : f.shape == 2 ? cudaLaunchKernelEx(&cfg, sart_fp_kernel<1, 8, 8, 2>, A)
@@ -989,16 +1025,23 @@ extern "C" int udev_sart_bp(udev *d, const udev_geom *g, int angle, float sn, fl
     /* 32-row tiles while they leave fewer than ~4 CTAs per SM, else 64-row */
     const bool tall = (long long) udev_div_up(n, kBpTileW) * udev_div_up(n, 64) * n_slices >= 4LL * udev_sm_count(d);
     dim3 grid(udev_div_up(n, kBpTileW), udev_div_up(n, tall ? 64 : 32), (unsigned int) n_slices);
-    if (tall) {
-        if (place == 1)
-            sart_bp_kernel<true, 8><<<grid, dim3(32, 8), 0, d->stream>>>(A);
-        else
-            sart_bp_kernel<false, 8><<<grid, dim3(32, 8), 0, d->stream>>>(A);
-    } else {
-        if (place == 1)
-            sart_bp_kernel<true, 4><<<grid, dim3(32, 8), 0, d->stream>>>(A);
-        else
-            sart_bp_kernel<false, 4><<<grid, dim3(32, 8), 0, d->stream>>>(A);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(32, 8, 1);
+    cfg.stream = d->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = sart_pdl(d, n, n_slices) ? 1 : 0;
+    const cudaError_t e = tall ? (place == 1 ? cudaLaunchKernelEx(&cfg, sart_bp_kernel<true, 8>, A)
+                                             : cudaLaunchKernelEx(&cfg, sart_bp_kernel<false, 8>, A))
+                               : (place == 1 ? cudaLaunchKernelEx(&cfg, sart_bp_kernel<true, 4>, A)
+                                             : cudaLaunchKernelEx(&cfg, sart_bp_kernel<false, 4>, A));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        udev_set_error(d, "sart_bp_kernel launch: %s", cudaGetErrorString(e));
+        return UFOIR_ERR_CUDA;
     }
     return udev_after_launch(d, "sart_bp_kernel");
 }
