@@ -1,12 +1,12 @@
 """The allocation-free L1-norm entry point, through the C ABI.
 
-ufoir_l1_norm_fp64_noalloc is for callers that cannot allocate device
-memory where they need the norm (inside their own stream capture, under a
-device-memory budget owned by another allocator, in loops that must not
-touch the allocator). It keeps its partial sums in a fixed device array, so
-these checks run it twice in a row (the second call reuses the array that
-the first call filled) and compare each result with the allocating
-ufoir_l1_norm in FP64 mode. This file is collected last so that a failure
+ufoir_l1_norm_fp64_noalloc is for callers that must not allocate device
+memory where they need the norm (their GPU memory is owned by another
+allocator or held to a hard per-process limit, or they run loops that must
+not take the allocator's locks). It keeps its partial sums in a fixed
+device array, so these checks run it twice in a row (the second call reuses
+the array that the first call filled) and compare each result with the
+allocating ufoir_l1_norm in FP64 mode. This file is collected last so that a failure
 here comes after every other test has run; it also passes on its own.
 """
 import ctypes as C

@@ -419,7 +419,13 @@ __global__ void __launch_bounds__(32 * W, MINB) sart_fp_kernel(SartFpArgs P)
     const int s0 = g * 64 + lane, s1 = s0 + 32;
     pdl_launch_next();
 
-    /* CTA 0 fetches its rays' src and w early */
+    /* CTA 0 fetches its rays' src and w early, before the grid dependency
+     * wait. This is safe because src (the sinogram b) and w (the ray weights
+     * R) are written only by kernels that do not trigger their dependents
+     * early: every padded sweep starts with sart_copy_kernel, launched
+     * without programmatic dependency, after the last write to b and R. A
+     * kernel that updates b or R inside the sweep must move these loads
+     * after pdl_wait_previous(). */
     const int sr = g * 64 + (int) threadIdx.x;
     const bool writer = rank == 0 && threadIdx.x < 64 && sr < n;
     const size_t oidx = (size_t) slice * P.sino_stride + (size_t) P.angle * n + sr;
