@@ -100,6 +100,14 @@ UFOIR_API uint64_t ufoir_ctx_kernel_launches(const ufoir_ctx *ctx);
 /* CUDA-event timer on the context's stream: begin records a start event,
  * end records a stop event, waits for it and returns the elapsed device time. */
 UFOIR_API int ufoir_ctx_timer_begin(ufoir_ctx *ctx);
+/* Testing the device-side bounded waits (no reference counterpart; the
+ * reference logs OpenCL errors and continues, src/core/ufo-ir-basic-ops.c:60-64):
+ * the next tiled forward projection launched on this context leaves the
+ * shared-memory bulk copy of row chunk `chunk` unissued in every CTA (-1
+ * cancels). Its waits then run out after their 250 ms limit, the kernel
+ * drains its other copies, writes nothing and records the timeout, and the
+ * call returns UFOIR_ERR_TIMEOUT; the context stays usable. One-shot. */
+UFOIR_API int ufoir_ctx_inject_copy_timeout(ufoir_ctx *ctx, int chunk);
 UFOIR_API int ufoir_ctx_timer_end(ufoir_ctx *ctx, float *ms);
 
 /* ------------------------------------------------------------------------ */
@@ -256,6 +264,23 @@ UFOIR_API int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params 
 UFOIR_API int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *p,
                                     const float *sino, const size_t sino_dims[2], float *vol,
                                     size_t n_slices);
+/* ASD-POCS with its internal state returned, for inspection and tests. The
+ * reference's output is copied before the TV stage of each outer iteration
+ * (src/tasks/ufo-ir-asdpocs-task.c:468), so the TV steepest descent
+ * (ufo_math_tvstd_method_process_real, :550-580, kernel l1_grad of
+ * src/kernels/ufo-math-tvstd-method.cl:5-57) shows only in these locals of
+ * process() (:411-509):
+ *   x_tv     (may be NULL) n_slices volumes, host or device: x after the 20 TV
+ *            sub-steps of the last outer iteration;
+ *   scalars  (may be NULL) n_slices records: dp, dd, dg and dtgv as they
+ *            stand when process() returns (dtgv after the :501-503 update).
+ * vol and every other argument are as in ufoir_asdpocs_process. */
+typedef struct {
+    float dp, dd, dg, dtgv;
+} ufoir_asdpocs_scalars;
+UFOIR_API int ufoir_asdpocs_process_ex(ufoir_projector *proj, const ufoir_asdpocs_params *p,
+                                       const float *sino, const size_t sino_dims[2], float *vol,
+                                       size_t n_slices, float *x_tv, ufoir_asdpocs_scalars *scalars);
 /* Split-Bregman TV: src/tasks/ufo-ir-sbtv-task.c:230-635. The reference
  * min-max-normalises its input sinogram in place (:239); this call leaves
  * the caller's sinogram untouched and works on a normalised copy. */
@@ -264,9 +289,10 @@ UFOIR_API int ufoir_sbtv_process(ufoir_projector *proj, const ufoir_sbtv_params 
                                  size_t n_slices);
 
 /* ------------------------------------------------------------------------ */
-/* Resident batched SIRT: the persistent form of ufoir_sirt_process for     */
-/* many slices whose data stay in HBM. Creation computes the weights (once, */
-/* shared by all slices), zeroes the volumes and captures one iteration     */
+/* Resident batched SIRT: ufoir_sirt_process split into setup and replayed */
+/* iterations, for many slices whose data stay in HBM. Creation computes   */
+/* the weights (once, shared by all slices), zeroes the volumes and        */
+/* captures one iteration                                                   */
 /* (transpose + FP + BP launches over all slices) as a CUDA graph; run()    */
 /* replays it. Results equal ufoir_sirt_process with the same iteration     */
 /* count, bit for bit. No reference counterpart beyond sirt-task.c:164-222: */
@@ -296,14 +322,19 @@ UFOIR_API void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b);
 /* and has no serving mode; this is the continuous-batching counterpart of  */
 /* calling ufoir_*_process once per job.                                    */
 /*                                                                          */
-/* A worker thread admits queued jobs in arrival order while the HBM budget */
-/* and the active-job limit allow, keeps each admitted job's sinogram and   */
-/* iterate resident on the device, and advances every active job a quantum */
-/* at a time on the job's own CUDA stream, so the work of different jobs    */
+/* A worker thread admits queued jobs while the HBM budget and the         */
+/* active-job limit allow, keeps each admitted job's sinogram and iterate   */
+/* resident on the device, and advances every active job a quantum at a    */
+/* time on the job's own CUDA stream, so the work of different jobs         */
 /* overlaps on the GPU and a job is admitted as soon as memory frees up.    */
 /* Each job runs exactly the kernels of the plain call, so its result does  */
-/* not depend on what else is in flight. Policy ONE_AT_A_TIME admits one    */
-/* job at a time (the plain per-job path) for comparison.                   */
+/* not depend on what else is in flight. Admission (CONTINUOUS) is in       */
+/* arrival order, except that a job that does not fit the budget may be    */
+/* passed by later jobs that do until it has waited admit_age_ms; quanta   */
+/* go to the admitted jobs with the least remaining work. For comparison,  */
+/* ONE_AT_A_TIME runs one job at a time in arrival order (the plain per-job */
+/* path) and SJF_ONE_AT_A_TIME one job at a time, the queued job with the   */
+/* least work first (the ordering of CONTINUOUS without its overlap).       */
 /* ------------------------------------------------------------------------ */
 /* Methods of a job or graph; the serve loop runs SART, SIRT and ASD-POCS. */
 enum { UFOIR_METHOD_SART = 0, UFOIR_METHOD_SIRT = 1, UFOIR_METHOD_ASDPOCS = 2, UFOIR_METHOD_SBTV = 3 };
@@ -314,7 +345,7 @@ enum {
     UFOIR_JOB_FAILED = 3,
     UFOIR_JOB_CANCELLED = 4
 };
-enum { UFOIR_SERVE_CONTINUOUS = 0, UFOIR_SERVE_ONE_AT_A_TIME = 1 };
+enum { UFOIR_SERVE_CONTINUOUS = 0, UFOIR_SERVE_ONE_AT_A_TIME = 1, UFOIR_SERVE_SJF_ONE_AT_A_TIME = 2 };
 
 typedef struct {
     int method;                       /* UFOIR_METHOD_* */
@@ -334,6 +365,8 @@ typedef struct {
     unsigned int fail_allocation_every; /* testing: make every k-th job allocation fail (0 = off) */
     unsigned int max_running;         /* CONTINUOUS: jobs with work in flight at once, the ones
                                          with the least remaining work first; 0 = 4 */
+    unsigned int admit_age_ms;        /* CONTINUOUS: how long a queued job that does not fit the
+                                         budget may be passed by later jobs; 0 = 2000 */
 } ufoir_serve_config;
 
 typedef struct {
@@ -383,34 +416,14 @@ UFOIR_API int ufoir_l1_norm(ufoir_ctx *ctx, const float *v, size_t w, size_t h, 
                             float *out);
 UFOIR_API int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, size_t w,
                                 size_t h, int norm_mode, float *out);
+/* The TV subgradient of ASD-POCS's steepest-descent stage: kernel l1_grad
+ * (src/kernels/ufo-math-tvstd-method.cl:5-57, launched over (w, h) by
+ * src/tasks/ufo-ir-asdpocs-task.c:563-571) on n_slices images of w x h
+ * floats stored back to back: the 7-point stencil with EPS 1e-3 and a zero
+ * border. v and out: host or device memory. */
+UFOIR_API int ufoir_tv_gradient(ufoir_ctx *ctx, const float *v, size_t w, size_t h, size_t n_slices,
+                                float *out);
 
-/* ------------------------------------------------------------------------ */
-/* Allocation-free L1 norm. No counterpart in the reference.                */
-/*                                                                          */
-/* For callers that cannot allocate device memory at the point where they  */
-/* need the norm: code running while its own stream is captured into a CUDA */
-/* graph (allocation is not capturable), code whose GPU memory belongs to   */
-/* another allocator or sits under a hard per-process limit, and loops that */
-/* must not take the allocator's locks. It computes what ufoir_l1_norm      */
-/* computes with UFOIR_NORM_FP64 (same result bit for bit), for n_slices     */
-/* slices of `count` floats stored back to back, but keeps its partial sums */
-/* in a fixed device array inside the library instead of allocating:       */
-/*   - the array holds UFOIR_NOALLOC_MAX_SLICES x 512 doubles (256 KiB) and  */
-/*     every GPU that loads the library keeps it until the process exits;   */
-/*   - n_slices > UFOIR_NOALLOC_MAX_SLICES is rejected with                 */
-/*     UFOIR_ERR_INVALID and nothing is launched;                           */
-/*   - the first call on a device looks up that array's device address      */
-/*     (cudaGetSymbolAddress, once per device, with the caller's current    */
-/*     device); make that first call before any stream capture;             */
-/*   - all calls share the array, so calls whose work overlaps on the GPU   */
-/*     (different streams without ordering between them) race and give      */
-/*     wrong results; each call overwrites every partial it reads, so       */
-/*     nothing needs clearing between calls.                                */
-/* d_v (input) and d_out (n_slices floats, output) are device memory of the */
-/* current device; the work is queued on `stream` (a cudaStream_t, NULL =   */
-/* the default stream) and d_out is valid once the stream reaches it. No   */
-/* cudaMalloc, cudaFree or allocating library call is made.                 */
-/* ------------------------------------------------------------------------ */
 /* Measurement (no counterpart in the reference): the interpolated-sample  */
 /* rate ceiling of the device, i.e. the forward projector's exact per-      */
 /* sample instruction sequence run from shared memory by every SM with no   */
@@ -421,6 +434,39 @@ UFOIR_API int ufoir_sample_ceiling(ufoir_ctx *ctx, double *samples_per_s);
 /* coordinate, floor, two window taps per pixel, filter and sum).          */
 UFOIR_API int ufoir_sample_ceiling_bp(ufoir_ctx *ctx, double *samples_per_s);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free L1 norm. No counterpart in the reference.                */
+/*                                                                          */
+/* For callers that must not allocate device memory where they need the    */
+/* norm: code whose GPU memory belongs to another allocator (a host         */
+/* framework's pooling allocator) or sits under a hard per-process limit    */
+/* (an MPS client with a set memory limit), where a library must not grow   */
+/* its own footprint, and loops that must not take the allocator's locks or */
+/* the implicit synchronisation cudaMalloc/cudaFree can cause. It computes  */
+/* what ufoir_l1_norm computes with UFOIR_NORM_FP64 (same result bit for    */
+/* bit), for n_slices slices of `count` floats stored back to back, but     */
+/* keeps its partial sums in a fixed device array inside the library       */
+/* instead of allocating:                                                   */
+/*   - the array holds UFOIR_NOALLOC_MAX_SLICES x 512 doubles (256 KiB) and  */
+/*     every GPU that loads the library keeps it until the process exits;   */
+/*   - n_slices > UFOIR_NOALLOC_MAX_SLICES is rejected with                 */
+/*     UFOIR_ERR_INVALID and nothing is launched;                           */
+/*   - the first call in a CUDA context (normally: the first call on a      */
+/*     device) looks up the array's device address there with               */
+/*     cudaGetSymbolAddress, with that context current, and caches it per   */
+/*     context; make that first call before any stream capture. A device    */
+/*     reset gives a new context, whose first call looks the address up     */
+/*     again;                                                               */
+/*   - all calls share the array, so calls whose work overlaps on the GPU   */
+/*     (different streams without ordering between them) race and give      */
+/*     wrong results; each call overwrites every partial it reads, so       */
+/*     nothing needs clearing between calls.                                */
+/* d_v (input) and d_out (n_slices floats, output) are device memory of the */
+/* current device; the work is queued on `stream` (a cudaStream_t, NULL =   */
+/* the default stream) and d_out is valid once the stream reaches it. No   */
+/* cudaMalloc, cudaFree or allocating library call is made. The status is   */
+/* this call's own: an error the caller left pending is not reported.       */
+/* ------------------------------------------------------------------------ */
 #define UFOIR_NOALLOC_MAX_SLICES 64
 UFOIR_API int ufoir_l1_norm_fp64_noalloc(const float *d_v, size_t count, unsigned int n_slices,
                                          float *d_out, void *stream);

@@ -242,7 +242,13 @@ void oracle_sirt_iterate(const oracle_kernels *k, oracle_projector *p, unsigned 
 void oracle_asdpocs(const oracle_kernels *k, oracle_projector *p, const oracle_asdpocs_params *prm,
                     const float *sino, float *vol, float *x_internal)
 {
-    asdpocs_impl_f(k, p, prm, sino, vol, x_internal);
+    asdpocs_impl_f(k, p, prm, sino, vol, x_internal, NULL);
+}
+
+void oracle_asdpocs_state(const oracle_kernels *k, oracle_projector *p, const oracle_asdpocs_params *prm,
+                          const float *sino, float *vol, float *x_internal, float scalars[4])
+{
+    asdpocs_impl_f(k, p, prm, sino, vol, x_internal, scalars);
 }
 
 void oracle_sbtv(const oracle_kernels *k, oracle_projector *p, const oracle_sbtv_params *prm,
@@ -306,7 +312,15 @@ void oracle_asdpocs_d(oracle_projector *p, const oracle_asdpocs_params *prm,
 {
     oracle_asdpocs_params q = *prm;
     q.norm_mode = ORACLE_NORM_FP64;
-    asdpocs_impl_d(&port_d, p, &q, sino, vol, x_internal);
+    asdpocs_impl_d(&port_d, p, &q, sino, vol, x_internal, NULL);
+}
+
+void oracle_asdpocs_d_state(oracle_projector *p, const oracle_asdpocs_params *prm, const double *sino,
+                            double *vol, double *x_internal, double scalars[4])
+{
+    oracle_asdpocs_params q = *prm;
+    q.norm_mode = ORACLE_NORM_FP64;
+    asdpocs_impl_d(&port_d, p, &q, sino, vol, x_internal, scalars);
 }
 
 void oracle_sbtv_d(oracle_projector *p, const oracle_sbtv_params *prm, double *sino, double *vol)

@@ -170,6 +170,11 @@ typedef struct {
 void oracle_asdpocs(const oracle_kernels *k, oracle_projector *p,
                     const oracle_asdpocs_params *prm, const float *sino,
                     float *vol, float *x_internal);
+/* The same, and scalars[0..3] receive the locals dp, dd, dg and dtgv of
+ * process() as they stand at its return (asdpocs-task.c:411-509). */
+void oracle_asdpocs_state(const oracle_kernels *k, oracle_projector *p,
+                          const oracle_asdpocs_params *prm, const float *sino,
+                          float *vol, float *x_internal, float scalars[4]);
 
 typedef struct {
     unsigned int num_iterations;
@@ -199,6 +204,9 @@ void oracle_sart_d(oracle_projector *p, unsigned int iters, float relaxation_fac
                    const double *sino, double *vol);
 void oracle_asdpocs_d(oracle_projector *p, const oracle_asdpocs_params *prm,
                       const double *sino, double *vol, double *x_internal);
+void oracle_asdpocs_d_state(oracle_projector *p, const oracle_asdpocs_params *prm,
+                            const double *sino, double *vol, double *x_internal,
+                            double scalars[4]);
 void oracle_sbtv_d(oracle_projector *p, const oracle_sbtv_params *prm,
                    double *sino, double *vol);
 

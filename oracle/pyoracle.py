@@ -80,9 +80,44 @@ class Kernels(C.Structure):
                 ("dyt", C.CFUNCTYPE(None, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_long, C.c_long))]
 
 
+# The reference's four OpenCL kernel files, compiled through clshim.hpp into
+# _ref/libufoir_ref.so. Where the ufo-ir tree is present they are staged,
+# unmodified, into the git-ignored baseline/_ref/kernels so that the build on
+# a machine without the tree (the GPU host) compiles the same sources.
+REF_TREE_KERNELS = "/root/reference/src/kernels"
+STAGED_KERNELS = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "kernels")
+REF_KERNEL_FILES = ("projector-parallel-joseph.cl", "ufo-ir-basic-ops.cl", "ufo-math-tvstd-method.cl",
+                    "ufo-ir-gradient-processor.cl")
+
+
+def reference_kernel_dir():
+    """Directory of the reference kernel sources: $UFO_IR_REF, else the ufo-ir
+    tree (staged into baseline/_ref/kernels on the way), else the staged copy,
+    else None."""
+    env = os.environ.get("UFO_IR_REF")
+    if env:
+        return env
+    if all(os.path.exists(os.path.join(REF_TREE_KERNELS, f)) for f in REF_KERNEL_FILES):
+        import shutil
+        os.makedirs(STAGED_KERNELS, exist_ok=True)
+        for f in REF_KERNEL_FILES:
+            dst = os.path.join(STAGED_KERNELS, f)
+            src = os.path.join(REF_TREE_KERNELS, f)
+            if not os.path.exists(dst) or open(src, "rb").read() != open(dst, "rb").read():
+                shutil.copyfile(src, dst)
+        return STAGED_KERNELS
+    if all(os.path.exists(os.path.join(STAGED_KERNELS, f)) for f in REF_KERNEL_FILES):
+        return STAGED_KERNELS
+    return None
+
+
 def build(quiet: bool = True) -> None:
-    """Compile the oracle (and the reference kernels when the reference tree exists)."""
-    out = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    """Compile the oracle (and the reference kernels when their sources are available)."""
+    cmd = ["make", "-s", "-C", HERE]
+    ref_dir = reference_kernel_dir()
+    if ref_dir:
+        cmd.append("UFO_IR_REF=" + ref_dir)
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:
@@ -135,6 +170,7 @@ def _declare(lib):
     lib.oracle_sirt_weights.argtypes = [kp, pp, f32p, f32p]
     lib.oracle_sirt_iterate.argtypes = [kp, pp, C.c_uint, C.c_float, f32p, f32p, f32p, f32p]
     lib.oracle_asdpocs.argtypes = [kp, pp, C.POINTER(AsdpocsParams), f32p, f32p, f32p]
+    lib.oracle_asdpocs_state.argtypes = [kp, pp, C.POINTER(AsdpocsParams), f32p, f32p, f32p, f32p]
     lib.oracle_sbtv.argtypes = [kp, pp, C.POINTER(SbtvParams), f32p, f32p]
     for name in ("oracle_l1_norm", "oracle_l1_norm_fp64"):
         getattr(lib, name).argtypes = [f32p, C.c_ulong, C.c_ulong]
@@ -147,6 +183,7 @@ def _declare(lib):
     lib.oracle_sirt_d.argtypes = [pp, C.c_uint, C.c_float, f64p, f64p]
     lib.oracle_sart_d.argtypes = [pp, C.c_uint, C.c_float, f64p, f64p]
     lib.oracle_asdpocs_d.argtypes = [pp, C.POINTER(AsdpocsParams), f64p, f64p, f64p]
+    lib.oracle_asdpocs_d_state.argtypes = [pp, C.POINTER(AsdpocsParams), f64p, f64p, f64p, f64p]
     lib.oracle_sbtv_d.argtypes = [pp, C.POINTER(SbtvParams), f64p, f64p]
     lib.oracle_siddon_forward.argtypes = [C.c_uint, C.c_uint, f32p, f32p, C.c_float, f32p, f64p]
     lib.oracle_siddon_backward.argtypes = [C.c_uint, C.c_uint, f32p, f32p, C.c_float, f32p, f64p]
@@ -268,6 +305,16 @@ def asdpocs(p: Projector, sino, prm: AsdpocsParams, which="port"):
     return vol, xint
 
 
+def asdpocs_state(p: Projector, sino, prm: AsdpocsParams, which="port"):
+    """ASD-POCS: (output, post-TV x of the last outer iteration, {dp, dd, dg, dtgv})."""
+    vol = np.zeros((p.n_dets, p.n_dets), np.float32)
+    xint = np.zeros_like(vol)
+    sc = np.zeros(4, np.float32)
+    port_lib().oracle_asdpocs_state(kernels(which), C.byref(p), C.byref(prm), _f32(sino), _f32(vol), _f32(xint),
+                                    _f32(sc))
+    return vol, xint, dict(zip(("dp", "dd", "dg", "dtgv"), (float(v) for v in sc)))
+
+
 def sbtv_params(**kw) -> SbtvParams:
     d = dict(num_iterations=10, lambda_=0.1, mu=0.5, norm_mode=NORM_COMPAT)
     d.update(kw)
@@ -326,6 +373,15 @@ def asdpocs_d(p: Projector, sino, prm: AsdpocsParams):
     port_lib().oracle_asdpocs_d(C.byref(p), C.byref(prm),
                                 _f64(np.ascontiguousarray(sino, np.float64)), _f64(vol), _f64(xint))
     return vol, xint
+
+
+def asdpocs_d_state(p: Projector, sino, prm: AsdpocsParams):
+    vol = np.zeros((p.n_dets, p.n_dets), np.float64)
+    xint = np.zeros_like(vol)
+    sc = np.zeros(4, np.float64)
+    port_lib().oracle_asdpocs_d_state(C.byref(p), C.byref(prm),
+                                      _f64(np.ascontiguousarray(sino, np.float64)), _f64(vol), _f64(xint), _f64(sc))
+    return vol, xint, dict(zip(("dp", "dd", "dg", "dtgv"), (float(v) for v in sc)))
 
 
 def sbtv_d(p: Projector, sino, prm: SbtvParams):

@@ -46,6 +46,31 @@ def test_oracle_matches_golden_methods(oracle):
     assert np.float32(oracle.dot_product(d["a"], d["b"])) == d["dot"]
 
 
+def test_oracle_matches_golden_tv(oracle):
+    """The port's l1_grad (ufo-math-tvstd-method.cl:5-57) on one-row, one-column,
+    constant, step and random images, and ASD-POCS's post-TV iterate and
+    scalars dp, dd, dg, dtgv after 5 outer iterations, against the fixture the
+    reference kernels produced."""
+    d = np.load(os.path.join(GOLDEN, "tv_n40_a30.npz"))
+    k = oracle.kernels("port").contents
+    for key in [f[len("g_in_"):] for f in d.files if f.startswith("g_in_")]:
+        a = d["g_in_" + key]
+        g = np.zeros_like(a)
+        k.l1_grad(oracle.image(a), oracle.image(g))
+        assert np.array_equal(g, d["g_out_" + key]), key
+    n, na, step = int(d["n"]), int(d["na"]), np.float32(d["step"])
+    prm = oracle.asdpocs_params(num_iterations=int(d["outer"]), sart_iterations=int(d["sart_iterations"]),
+                                norm_mode=oracle.NORM_COMPAT)
+    vol, x, sc = oracle.asdpocs_state(oracle.projector(n, na, step), d["sino"], prm)
+    assert np.array_equal(vol, d["asdpocs"]) and np.array_equal(x, d["asdpocs_x"])
+    assert np.array_equal(np.array([sc["dp"], sc["dd"], sc["dg"], sc["dtgv"]], np.float32), d["scalars"])
+    # the TV stage changed x, and the dtgv reduction was taken
+    assert not np.array_equal(vol, x)
+    prm1 = oracle.asdpocs_params(num_iterations=1, sart_iterations=int(d["sart_iterations"]),
+                                 norm_mode=oracle.NORM_COMPAT)
+    assert sc["dtgv"] < oracle.asdpocs_state(oracle.projector(n, na, step), d["sino"], prm1)[2]["dtgv"]
+
+
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
                                                      "libufoir_ref.so")),
                     reason="reference kernels (oracle/_ref) are built only where the reference tree exists")

@@ -757,8 +757,26 @@ int ufoir__asd_outer(ufoir__asd_state *s)
     return UFOIR_OK;
 }
 
+static int asdpocs_run(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
+                       const size_t dims[2], float *vol, size_t n_slices, float *x_tv,
+                       ufoir_asdpocs_scalars *scalars);
+
 int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
                           const size_t dims[2], float *vol, size_t n_slices)
+{
+    return asdpocs_run(proj, prm, sino, dims, vol, n_slices, NULL, NULL);
+}
+
+int ufoir_asdpocs_process_ex(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
+                             const size_t dims[2], float *vol, size_t n_slices, float *x_tv,
+                             ufoir_asdpocs_scalars *scalars)
+{
+    return asdpocs_run(proj, prm, sino, dims, vol, n_slices, x_tv, scalars);
+}
+
+static int asdpocs_run(ufoir_projector *proj, const ufoir_asdpocs_params *prm, const float *sino,
+                       const size_t dims[2], float *vol, size_t n_slices, float *x_tv,
+                       ufoir_asdpocs_scalars *scalars)
 {
     if (!proj || !prm || !sino || !vol || !dims)
         return UFOIR_ERR_INVALID;
@@ -770,7 +788,8 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
     if (rc)
         return rc;
     const size_t n = proj->n_dets, nv = n * n, ns = n * proj->n_angles;
-    ufoir_buf bb = {0}, bo = {0};
+    ufoir_buf bb = {0}, bo = {0}, bx = {0};
+    float *hs = NULL;
     ufoir__asd_state st;
     memset(&st, 0, sizeof(st));
     st.p = proj;
@@ -781,10 +800,35 @@ int ufoir_asdpocs_process(ufoir_projector *proj, const ufoir_asdpocs_params *prm
         UFOIR_TRY(ufoir__asd_outer(&st));
     UFOIR_TRY(udev_take_kernel_error(ctx->dev));
     UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
+    if (x_tv) {
+        /* the iterate after the last outer iteration's TV sub-steps */
+        UFOIR_TRY(ufoir__buf_in(ctx, &bx, x_tv, nv * n_slices, 0));
+        UFOIR_TRY(udev_memcpy_async(ctx->dev, bx.dev, st.x, nv * n_slices * sizeof(float)));
+        UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
+    }
+    if (scalars) {
+        const size_t S = n_slices;
+        hs = (float *) malloc(sizeof(float) * 4 * S);
+        if (!hs) {
+            rc = ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+            goto done;
+        }
+        /* dp, dd, dg and dtgv are consecutive runs of S floats */
+        UFOIR_TRY(udev_memcpy_async(ctx->dev, hs, st.dsc.dp, sizeof(float) * 4 * S));
+        UFOIR_TRY(udev_sync(ctx->dev));
+        for (size_t i = 0; i < S; i++) {
+            scalars[i].dp = hs[i];
+            scalars[i].dd = hs[S + i];
+            scalars[i].dg = hs[2 * S + i];
+            scalars[i].dtgv = hs[3 * S + i];
+        }
+    }
 done:
+    free(hs);
     ufoir__asd_release(&st);
     ufoir__buf_release(ctx, &bb);
     ufoir__buf_release(ctx, &bo);
+    ufoir__buf_release(ctx, &bx);
     udev_sync(ctx->dev);
     return rc;
 }
@@ -1235,6 +1279,26 @@ int ufoir_dot_product(ufoir_ctx *ctx, const float *a, const float *b, size_t w, 
 done:
     ufoir__buf_release(ctx, &ba);
     ufoir__buf_release(ctx, &bb);
+    udev_sync(ctx->dev);
+    return rc;
+}
+
+int ufoir_tv_gradient(ufoir_ctx *ctx, const float *v, size_t w, size_t h, size_t n_slices, float *out)
+{
+    if (!ctx || !v || !out || w == 0 || h == 0 || n_slices == 0)
+        return UFOIR_ERR_INVALID;
+    if (w > (size_t) INT32_MAX || h > (size_t) INT32_MAX || n_slices > 65535)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "tv_gradient: %zu x %zu x %zu is too large", w, h, n_slices);
+    ufoir_buf bi = {0}, bo = {0};
+    int rc;
+    UFOIR_TRY(ufoir__buf_in(ctx, &bi, v, w * h * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bo, out, w * h * n_slices, 0));
+    UFOIR_TRY(udev_l1_grad(ctx->dev, bi.dev, bo.dev, (int) w, (int) h, (int) n_slices));
+    UFOIR_TRY(udev_take_kernel_error(ctx->dev));
+    UFOIR_TRY(ufoir__buf_out(ctx, &bo, 1));
+done:
+    ufoir__buf_release(ctx, &bi);
+    ufoir__buf_release(ctx, &bo);
     udev_sync(ctx->dev);
     return rc;
 }

@@ -68,6 +68,10 @@ class AsdpocsParams(C.Structure):
                 ("norm_mode", C.c_int)]
 
 
+class AsdpocsScalars(C.Structure):
+    _fields_ = [("dp", C.c_float), ("dd", C.c_float), ("dg", C.c_float), ("dtgv", C.c_float)]
+
+
 class SbtvParams(C.Structure):
     _fields_ = [("num_iterations", C.c_uint), ("lambda_", C.c_float), ("mu", C.c_float),
                 ("norm_mode", C.c_int)]
@@ -89,6 +93,7 @@ class Graph(C.Structure):
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = 0, 1, 2, 3, 4
 SERVE_CONTINUOUS = 0
 SERVE_ONE_AT_A_TIME = 1
+SERVE_SJF_ONE_AT_A_TIME = 2
 
 
 class JobDesc(C.Structure):
@@ -98,7 +103,8 @@ class JobDesc(C.Structure):
 
 class ServeConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_uint), ("policy", C.c_int),
-                ("quantum", C.c_uint), ("fail_allocation_every", C.c_uint), ("max_running", C.c_uint)]
+                ("quantum", C.c_uint), ("fail_allocation_every", C.c_uint), ("max_running", C.c_uint),
+                ("admit_age_ms", C.c_uint)]
 
 
 class ServeStats(C.Structure):
@@ -135,6 +141,7 @@ EXPORTED = (
     "ufoir_serve_get_stats", "ufoir_serve_destroy", "ufoir_graph_parse", "ufoir_graph_load",
     "ufoir_graph_job_desc", "ufoir_graph_run", "ufoir_io_last_error", "ufoir_io_tiff_info", "ufoir_io_read_tiff",
     "ufoir_io_write_tiff", "ufoir_io_read_raw", "ufoir_io_write_raw", "ufoir_sample_ceiling", "ufoir_sample_ceiling_bp",
+    "ufoir_asdpocs_process_ex", "ufoir_tv_gradient", "ufoir_ctx_inject_copy_timeout",
 )
 
 
@@ -228,6 +235,10 @@ def _declare(L):
     L.ufoir_sample_ceiling_bp.argtypes = [vp, C.POINTER(C.c_double)]
     L.ufoir_l1_norm.argtypes = [vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
     L.ufoir_dot_product.argtypes = [vp, vp, vp, C.c_size_t, C.c_size_t, C.c_int, f32p]
+    L.ufoir_asdpocs_process_ex.argtypes = [vp, C.POINTER(AsdpocsParams), vp, szp, vp, C.c_size_t, vp,
+                                           C.POINTER(AsdpocsScalars)]
+    L.ufoir_tv_gradient.argtypes = [vp, vp, C.c_size_t, C.c_size_t, C.c_size_t, vp]
+    L.ufoir_ctx_inject_copy_timeout.argtypes = [vp, C.c_int]
 
 
 class DeviceArray:
@@ -559,6 +570,34 @@ def asdpocs(proj, sino, vol=None, **kw):
     return _run_method("asdpocs", proj, asdpocs_params(**kw), sino, vol)
 
 
+def asdpocs_state(proj, sino, vol=None, **kw):
+    """ASD-POCS returning (output, x after the last outer iteration's TV
+    sub-steps, [{dp, dd, dg, dtgv} per slice]) (ufoir_asdpocs_process_ex)."""
+    prm = asdpocs_params(**kw)
+    n_angles, n = _shape(sino)[-2:]
+    lead = _shape(sino)[:-2]
+    n_slices = int(np.prod(lead)) if lead else 1
+    if vol is None:
+        vol = np.zeros(lead + (n, n), np.float32)
+    x_tv = np.zeros(lead + (n, n), np.float32)
+    sc = (AsdpocsScalars * n_slices)()
+    dims = (C.c_size_t * 2)(n, n_angles)
+    proj.ctx._check(lib().ufoir_asdpocs_process_ex(proj.handle, C.byref(prm), _ptr(sino), dims, _ptr(vol),
+                                                   n_slices, _ptr(x_tv), sc))
+    return vol, x_tv, [dict(dp=r.dp, dd=r.dd, dg=r.dg, dtgv=r.dtgv) for r in sc]
+
+
+def tv_gradient(ctx, v, out=None):
+    """l1_grad on one image [h, w] or a stack [s, h, w] (ufoir_tv_gradient)."""
+    shp = _shape(v)
+    h, w = shp[-2:]
+    n_slices = int(np.prod(shp[:-2])) if len(shp) > 2 else 1
+    if out is None:
+        out = np.zeros(shp, np.float32)
+    ctx._check(lib().ufoir_tv_gradient(ctx.handle, _ptr(v), w, h, n_slices, _ptr(out)))
+    return out
+
+
 def sbtv(proj, sino, vol=None, **kw):
     return _run_method("sbtv", proj, sbtv_params(**kw), sino, vol)
 
@@ -581,10 +620,12 @@ class Server:
 
     def __init__(self, ctx: Context, hbm_budget: int = 0, max_active_jobs: int = 0,
                  policy: int = SERVE_CONTINUOUS, quantum: int = 1, fail_allocation_every: int = 0,
-                 max_running: int = 0):
+                 max_running: int = 0, admit_age_ms: int = 0):
         self.ctx = ctx
         cfg = ServeConfig()
         lib().ufoir_serve_config_init(C.byref(cfg))
+        if admit_age_ms:
+            cfg.admit_age_ms = admit_age_ms
         cfg.hbm_budget_bytes = hbm_budget
         if max_active_jobs:
             cfg.max_active_jobs = max_active_jobs
