@@ -87,6 +87,14 @@ uint64_t ufoir_ctx_kernel_launches(const ufoir_ctx *ctx)
     return ctx ? udev_launches(ctx->dev) : 0;
 }
 
+int ufoir_ctx_inject_copy_timeout(ufoir_ctx *ctx, int chunk)
+{
+    if (!ctx || chunk < -1)
+        return UFOIR_ERR_INVALID;
+    udev_inject_copy_skip(ctx->dev, chunk);
+    return UFOIR_OK;
+}
+
 int ufoir_ctx_timer_begin(ufoir_ctx *ctx)
 {
     if (!ctx)

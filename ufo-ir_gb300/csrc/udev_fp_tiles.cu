@@ -64,6 +64,7 @@ struct FpTileArgs {
     int wcols;             /* columns staged per row: pitch (whole rows), or a window of the CTA's rays */
     int wstride;           /* shared floats per staged row (wcols + 4 for windows: 2 zero slots) */
     int margin;            /* window margin in columns (the recurrence's drift and the filter's taps) */
+    int skip_chunk;        /* testing: row chunk whose copy is left unissued (-1 = none) */
     int *err;
 };
 
@@ -177,6 +178,10 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
     auto issue = [&](int ch) {
         const int r0 = ch * K, rows = min(K, n - r0);
         float *dst = stage0 + (ch & 1) * stage_floats;
+        /* testing (ufoir_ctx_inject_copy_timeout): leave this chunk's copy
+         * unissued, so that its waits run out and the error path runs */
+        if (ch == P.skip_chunk)
+            return;
         if (!win) {
             const uint32_t bytes = (uint32_t) (rows * pitch) * 4u;
             w0s[ch & 1] = 0;
@@ -221,7 +226,8 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
         const int st = ch & 1;
         if (ok) {
             ok = tma::mbar_wait(&bars[st], (uint32_t) ((ch >> 1) & 1), P.err, tma::kErrWaitTimeout);
-            waited = ch + 1;
+            if (ok)
+                waited = ch + 1;   /* chunks [0, waited) have landed */
         }
         const int r0 = ch * K;
         const int rows = min(K, n - r0);
@@ -318,7 +324,9 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
         }
     }
     if (!ok) {
-        /* a copy did not arrive in time: drain what was issued, write nothing */
+        /* a copy did not arrive in time: drain what was issued (from the
+         * first chunk this thread did not see land, the timed-out one
+         * included), write nothing */
         if (threadIdx.x == 0)
             for (int ch = waited; ch < issued; ++ch)
                 tma::mbar_wait(&bars[ch & 1], (uint32_t) ((ch >> 1) & 1), P.err, tma::kErrDrainTimeout);
@@ -522,6 +530,8 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
     A.w_stride = w_shared ? 0 : A.sino_stride;
     A.neg_zero = -0.0f;
     A.err = d->d_err;
+    A.skip_chunk = d->inject_skip_chunk;   /* one-shot test injection */
+    d->inject_skip_chunk = -1;
     /* Too few tiles to fill the GPU (one slice, few angles): split each
      * angle tile's detectors over up to 8 CTAs, with chunks small enough
      * for two CTAs per SM. Every CTA walks all rows; it stages only the

@@ -28,6 +28,7 @@ struct udev {
     cudaEvent_t ev_stop = nullptr;
     int *d_err = nullptr;           /* kernel error word (bounded-wait timeouts) */
     int *h_err = nullptr;
+    int inject_skip_chunk = -1;     /* testing: see udev_inject_copy_skip */
 };
 
 /* One-time kernel attribute setup (dynamic shared memory opt-in). */

@@ -313,6 +313,11 @@ int udev_take_kernel_error(udev *d)
     return UFOIR_ERR_CUDA;
 }
 
+void udev_inject_copy_skip(udev *d, int chunk)
+{
+    d->inject_skip_chunk = chunk < 0 ? -1 : chunk;
+}
+
 int udev_timer_begin(udev *d)
 {
     UDEV_BIND(d);
