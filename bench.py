@@ -15,8 +15,11 @@ relaxation_factor 0.25.
           ufoir_sirt_process on the 64 host sinograms with num-iterations 10
           (the plugin default), including the host->device copy of the
           sinograms and the device->host copy of the volumes.
-  --impl reference   the reference's CPU implementation of the path (the
-          oracle port of its kernels and host loop, all host threads).
+  --impl reference   the reference's CPU implementation of the path: its own
+          OpenCL kernel sources compiled for the host through the oracle's
+          OpenCL-C shim (oracle/_ref), driven by the oracle's restatement of
+          its host loop, all host threads (the C port where the kernel
+          sources are absent).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ufoir|reference]
                        [--methods] [--quick] [--no-serve] [--projector-models]
@@ -43,12 +46,12 @@ sys.path.insert(0, os.path.join(ROOT, "ufo-ir_gb300"))
 METRIC = "SIRT slice-iters/s @1024²×1200 ang; serve p50/p99 latency vs plain per-job path"
 N_DETS, N_ANGLES, PHANTOM, SLICES, I0, RELAX = 1448, 1200, 1024, 64, 1e5, 0.25
 E2E_ITERS = 10
-CPU_SAMPLE_ANGLES = 300
-# serve trace: the configured request mix, scaled to seconds of GPU time
-SERVE_JOBS = 48
+# serve trace: the configured request mix (job shapes, methods, iteration
+# counts, arrival rate, budget) with its first SERVE_JOBS jobs
+SERVE_JOBS = 12
+SERVE_TRACE_JOBS = 2000
 SERVE_RATE = 200.0
 SERVE_SIZES = ((256, 367), (512, 724), (1024, 1448), (2048, 2900))
-SERVE_ITER_SCALE = 25
 SERVE_BUDGET = 150 * 10**9
 SERVE_SEED = 5005
 
@@ -188,65 +191,89 @@ def make_inputs(ufoir, ctx, proj, rank, S):
     return d_sino, d_vol, noisy
 
 
-def cpu_baseline(noisy_slice):
-    """The oracle port (the reference's kernels and host loop restated in C,
-    OpenMP over the NDRange) on one slice, over CPU_SAMPLE_ANGLES of the angles."""
+def _cpu_oracle():
+    """The oracle (test infrastructure, used here only as the CPU baseline and
+    the checker) with all host threads; which = "ref" when the reference's
+    own kernels were built (oracle/_ref), else "port"."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
     threads = os.cpu_count() or 1
     pyoracle.set_threads(threads)
-    stride = N_ANGLES // CPU_SAMPLE_ANGLES
-    na = N_ANGLES // stride
-    step = np.float32(np.float32(np.pi / N_ANGLES) * stride)
-    sino = np.ascontiguousarray(noisy_slice[::stride][:na])
-    p = pyoracle.projector(N_DETS, na, step)
-    R, Cw = pyoracle.sirt_weights(p)
+    which = "ref" if pyoracle.ref_available() else "port"
+    return pyoracle, threads, which
+
+
+def _cpu_kind(which):
+    return "reference" if which == "ref" else "port"
+
+
+def _cpu_what(which):
+    return ("the reference's OpenCL kernels compiled for the host (oracle/_ref) + the oracle's host loop"
+            if which == "ref" else "the oracle's C port of the reference kernels and host loop")
+
+
+def cpu_baseline(noisy_slice, gpu_result=None):
+    """The reference's CPU path on one slice of the workload: one full SIRT
+    iteration (all 1200 angles). With gpu_result (slice 0 of the e2e call,
+    E2E_ITERS iterations), also the checker: the oracle's result and its FP64
+    twin's for the same call, and their relative L2 errors."""
+    pyoracle, threads, which = _cpu_oracle()
+    step = np.float32(np.pi / N_ANGLES)
+    sino = np.ascontiguousarray(noisy_slice, np.float32)
+    p = pyoracle.projector(N_DETS, N_ANGLES, step)
+    R, Cw = pyoracle.sirt_weights(p, which=which)
     x = np.zeros((N_DETS, N_DETS), np.float32)
     t0 = time.perf_counter()
-    pyoracle.sirt_iterate(p, sino, R, Cw, x, 1, RELAX)
+    pyoracle.sirt_iterate(p, sino, R, Cw, x, 1, RELAX, which=which)
     dt = time.perf_counter() - t0
-    frac = na / N_ANGLES
-    return {"value": frac / dt, "unit": "slice-iters/s", "cores": threads, "kind": "port",
-            "sample": f"1 slice {N_DETS}^2, one SIRT iteration over {na} of the {N_ANGLES} angles "
-                      f"(every {stride}th), {dt:.2f} s, rate scaled by {na}/{N_ANGLES}"}
+    out = {"value": 1.0 / dt, "unit": "slice-iters/s", "cores": threads, "kind": _cpu_kind(which),
+           "sample": f"1 slice {N_DETS}^2, one SIRT iteration over all {N_ANGLES} angles, {dt:.2f} s; "
+                     + _cpu_what(which)}
+    if gpu_result is not None:
+        want = pyoracle.sirt(pyoracle.projector(N_DETS, N_ANGLES, step), sino, E2E_ITERS, RELAX, which=which)
+        want_d = pyoracle.sirt_d(pyoracle.projector(N_DETS, N_ANGLES, step), sino, E2E_ITERS, RELAX)
+        g = np.asarray(gpu_result, np.float64)
+        out["accuracy"] = {
+            "result": f"slice 0 of the e2e call ({E2E_ITERS} SIRT iterations)", "checker": _cpu_what(which),
+            "rel_l2_vs_oracle": float(np.linalg.norm(g - want) / np.linalg.norm(want)),
+            "bit_exact_vs_oracle": bool(np.array_equal(gpu_result, want)),
+            "rel_l2_vs_fp64_twin": float(np.linalg.norm(g - want_d) / np.linalg.norm(want_d)),
+            "oracle_rel_l2_vs_fp64_twin": float(np.linalg.norm(want.astype(np.float64) - want_d) /
+                                                np.linalg.norm(want_d)),
+            "bar": "rel-L2 <= 1e-4 against the reference after the stated iterations"}
+    return out
 
 
 def run_reference(args, dist):
-    """--impl reference: the reference's CPU path (oracle port), rank 0 only."""
+    """--impl reference: the reference's CPU path, rank 0 only."""
     if dist.rank != 0:
         return None
     from ufoir import synth
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    pyoracle.build()
-    threads = os.cpu_count() or 1
-    pyoracle.set_threads(threads)
-    stride = N_ANGLES // CPU_SAMPLE_ANGLES
-    na = N_ANGLES // stride
-    step = np.float32(np.float32(np.pi / N_ANGLES) * stride)
+    pyoracle, threads, which = _cpu_oracle()
+    step = np.float32(np.pi / N_ANGLES)
     vol = synth.ellipse_phantom(N_DETS, PHANTOM, 10, seed=2000)
-    p = pyoracle.projector(N_DETS, na, step)
-    sino, _ = synth.poisson_noise(pyoracle.forward(p, vol), I0, seed=3000)
-    R, Cw = pyoracle.sirt_weights(p)
+    p = pyoracle.projector(N_DETS, N_ANGLES, step)
+    sino, _ = synth.poisson_noise(pyoracle.forward(p, vol, which=which), I0, seed=3000)
+    R, Cw = pyoracle.sirt_weights(p, which=which)
     x = np.zeros((N_DETS, N_DETS), np.float32)
     for _ in range(args.warmup):
-        pyoracle.sirt_iterate(p, sino, R, Cw, x, 1, RELAX)
+        pyoracle.sirt_iterate(p, sino, R, Cw, x, 1, RELAX, which=which)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        pyoracle.sirt_iterate(p, sino, R, Cw, x, 1, RELAX)
+        pyoracle.sirt_iterate(p, sino, R, Cw, x, 1, RELAX, which=which)
     dt = time.perf_counter() - t0
-    frac = na / N_ANGLES
-    value = args.steps * frac / dt
-    sample = (f"per step: 1 slice {N_DETS}^2, one SIRT iteration over {na} of the {N_ANGLES} angles "
-              f"(every {stride}th), rate scaled by {na}/{N_ANGLES}")
+    value = args.steps / dt
+    sample = (f"per step: 1 slice {N_DETS}^2 of the {SLICES}-slice workload, one SIRT iteration over all "
+              f"{N_ANGLES} angles; " + _cpu_what(which))
     return {"metric": METRIC, "value": value, "unit": "slice-iters/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "SIRT 1448^2 grid, 1200 angles (sampled), 1024^2 ellipse phantom",
+            "config": {"workload": f"SIRT, {N_DETS}^2 grid (1024^2 ellipse phantom), {N_ANGLES} angles, "
+                                   f"{N_DETS} bins, one slice per step",
                        "n_dets": N_DETS, "n_angles": N_ANGLES, "threads": threads},
-            "cpu_baseline": {"value": value, "unit": "slice-iters/s", "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "slice-iters/s", "cores": threads, "kind": _cpu_kind(which),
                              "sample": sample},
             "e2e": {"value": value, "unit": "slice-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -285,7 +312,7 @@ def run_ufoir(args, dist):
         e2e, per_job = end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S)
     serve = None
     if not args.quick and not args.no_serve and dist.rank == 0:
-        serve = serve_section(ufoir, ctx)
+        serve = serve_section(ufoir, ctx, args.serve_jobs)
     methods = methods_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
     models = projector_models_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
 
@@ -344,7 +371,8 @@ def run_ufoir(args, dist):
                       "l2": "inputs larger than L2 (about 3 GB resident working set per GPU)",
                       "parallelism": "replicas: slices sharded across ranks, no collective"},
            "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "roofline": roofline,
-           "kernel_ms": kernel_ms, "sample_rate": sample_rate, **per_job}
+           "kernel_ms": kernel_ms, "sample_rate": sample_rate,
+           **{k: v for k, v in per_job.items() if not k.startswith("_")}}
     if serve is not None:
         out["serve"] = serve
     if methods is not None:
@@ -352,7 +380,8 @@ def run_ufoir(args, dist):
     if models is not None:
         out["projector_models"] = models
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and not args.quick:
-        out["cpu_baseline"] = cpu_baseline(noisy[0])
+        out["cpu_baseline"] = cpu_baseline(noisy[0], per_job.pop("_e2e_slice0", None))
+    per_job.pop("_e2e_slice0", None)
     d_sino.close()
     d_vol.close()
     proj.close()
@@ -386,37 +415,40 @@ def end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S):
     t0 = time.perf_counter()
     ufoir.sirt(proj, d_sino, d_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
     batched_s = time.perf_counter() - t0
-    per_job = {"plain_per_job": {"value": jobs * E2E_ITERS / plain_s, "unit": "slice-iters/s",
+    per_job = {"_e2e_slice0": np.array(h_vol[0], copy=True),
+               "plain_per_job": {"value": jobs * E2E_ITERS / plain_s, "unit": "slice-iters/s",
                                  "how": f"{jobs} single-slice ufoir_sirt_process calls, {E2E_ITERS} iterations each"},
                "batched_call": {"value": S * E2E_ITERS / batched_s, "unit": "slice-iters/s",
                                 "how": f"one ufoir_sirt_process call on {S} slices, {E2E_ITERS} iterations"}}
     return e2e, per_job
 
 
-def serve_trace(ufoir, ctx):
-    """A scaled copy of the serve workload: the configured job distributions
-    (phantom side P in {256, 512, 1024, 2048} -> grid n in {367, 724, 1448,
-    2900}; angles U{90..1800}; method in {SART, SIRT, ASD-POCS}; iterations
-    U{10..200}) with Poisson arrivals at 200 jobs/s, cut to SERVE_JOBS jobs and
-    iterations / SERVE_ITER_SCALE so that one pass takes seconds."""
+def serve_trace(ufoir, ctx, n_jobs):
+    """The serve workload as configured: phantom side P in {256, 512, 1024,
+    2048} -> grid n in {367, 724, 1448, 2900}; angles U{90..1800}; method in
+    {SART, SIRT, ASD-POCS}; iterations U{10..200} (ASD-POCS: outer
+    iterations, inner SART num-iterations 10, the plugin default); Poisson
+    arrivals at 200 jobs/s. The first n_jobs jobs of the 2000-job trace are
+    run, unchanged."""
     from ufoir import synth
     rng = np.random.default_rng(SERVE_SEED)
     methods = (ufoir.METHOD_SART, ufoir.METHOD_SIRT, ufoir.METHOD_ASDPOCS)
     jobs, t, samples = [], 0.0, 0.0
     cache = {}
-    for i in range(SERVE_JOBS):
+    for i in range(n_jobs):
         t += float(rng.exponential(1.0 / SERVE_RATE))
         P, n = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
         na = int(rng.integers(90, 1801))
         method = methods[int(rng.integers(3))]
-        iters = max(1, int(round(int(rng.integers(10, 201)) / SERVE_ITER_SCALE)))
+        iters = int(rng.integers(10, 201))
         step = float(np.float32(np.pi / na))
         if n not in cache:
             cache[n] = synth.ellipse_phantom(n, P, 10, seed=SERVE_SEED + n)
         proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=1)
-        sino = np.zeros((na, n), np.float32)
-        proj.forward(cache[n], sino)
+        clean = np.zeros((na, n), np.float32)
+        proj.forward(cache[n], clean)
         proj.close()
+        sino, _ = synth.poisson_noise(clean, 1e5, seed=SERVE_SEED + i)
         if method == ufoir.METHOD_ASDPOCS:
             desc = ufoir.job_desc(method, n, na, step, asdpocs=dict(num_iterations=iters))
             per_iter = 10
@@ -438,25 +470,30 @@ def run_serve(ufoir, ctx, jobs, policy):
             if delay > 0:
                 time.sleep(delay)
             ids.append(srv.submit(desc, sino)[0])
-        rc = srv.drain(600000)
+        rc = srv.drain(3600000)
         st = srv.stats()
         st["wall_s"] = time.perf_counter() - t0
         st["drain_status"] = rc
     return st
 
 
-def serve_section(ufoir, ctx):
-    """The same scaled trace through the continuous-batching loop and through
-    the one-job-at-a-time loop (the plain per-job path)."""
-    jobs, samples = serve_trace(ufoir, ctx)
+def serve_section(ufoir, ctx, n_jobs):
+    """The configured trace's first n_jobs jobs through three policies:
+    one_at_a_time (the plain per-job path, arrival order), sjf_one_at_a_time
+    (one job at a time, least work first: the ordering of the continuous loop
+    without its overlap) and continuous (overlapping jobs on the GPU)."""
+    jobs, samples = serve_trace(ufoir, ctx, n_jobs)
     span = jobs[-1][0]
-    out = {"trace": {"jobs": len(jobs), "arrival": f"Poisson, {SERVE_RATE:g} jobs/s (seed {SERVE_SEED})",
+    out = {"trace": {"jobs": len(jobs),
+                     "cut": f"the first {len(jobs)} jobs of the configured {SERVE_TRACE_JOBS}-job trace, "
+                            "job shapes, methods and iteration counts unchanged",
+                     "arrival": f"Poisson, {SERVE_RATE:g} jobs/s (seed {SERVE_SEED})",
                      "offered_window_s": span, "offered_jobs_per_s": len(jobs) / span if span > 0 else None,
                      "offered_samples": samples,
                      "sizes": "phantom P in {256,512,1024,2048} -> grid n in {367,724,1448,2900}",
                      "angles": "U{90..1800}", "methods": "SART / SIRT / ASD-POCS (uniform)",
-                     "iterations": f"U{{10..200}} / {SERVE_ITER_SCALE} (rounded, >= 1); ASD-POCS: outer "
-                                   "iterations, inner SART num-iterations 10",
+                     "iterations": "U{10..200}; ASD-POCS: outer iterations, inner SART num-iterations 10",
+                     "noise": "Poisson, I0 = 1e5, log",
                      "hbm_budget_bytes": SERVE_BUDGET,
                      "mix": {m: sum(1 for j in jobs if j[3] == k) for m, k in
                              (("sart", ufoir.METHOD_SART), ("sirt", ufoir.METHOD_SIRT),
@@ -464,7 +501,9 @@ def serve_section(ufoir, ctx):
     keys = ("completed", "failed", "p50_latency_ms", "p99_latency_ms", "mean_latency_ms", "max_latency_ms",
             "p50_queue_ms", "p99_queue_ms", "throughput_jobs_per_s", "busy_seconds", "peak_hbm_bytes",
             "peak_active_jobs", "wall_s")
-    for name, pol in (("one_at_a_time", ufoir.SERVE_ONE_AT_A_TIME), ("continuous", ufoir.SERVE_CONTINUOUS)):
+    for name, pol in (("one_at_a_time", ufoir.SERVE_ONE_AT_A_TIME),
+                      ("sjf_one_at_a_time", ufoir.SERVE_SJF_ONE_AT_A_TIME),
+                      ("continuous", ufoir.SERVE_CONTINUOUS)):
         st = run_serve(ufoir, ctx, jobs, pol)
         out[name] = {k: st[k] for k in keys if k in st}
         out[name]["samples_per_s"] = samples / st["busy_seconds"] if st.get("busy_seconds") else None
@@ -596,6 +635,8 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="only the resident timed steps (skip e2e, per-job comparison, serve trace, CPU baseline)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serve trace")
+    ap.add_argument("--serve-jobs", type=int, default=SERVE_JOBS,
+                    help="jobs of the configured serve trace to run (its first ones)")
     ap.add_argument("--methods", action="store_true",
                     help="also time one call of each other configured method workload (C1, C2, C3a/b, C4)")
     ap.add_argument("--projector-models", action="store_true",

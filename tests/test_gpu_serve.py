@@ -44,11 +44,12 @@ def _solo(ufoir, ctx, desc, sino, kw):
     return out
 
 
-@pytest.mark.parametrize("policy", ["continuous", "one_at_a_time"])
+@pytest.mark.parametrize("policy", ["continuous", "one_at_a_time", "sjf_one_at_a_time"])
 def test_results_in_the_mix_equal_results_alone(ufoir_lib, gpu_ctx, oracle, policy):
     ufoir = ufoir_lib
     jobs = _jobs(ufoir, oracle)
-    pol = ufoir.SERVE_CONTINUOUS if policy == "continuous" else ufoir.SERVE_ONE_AT_A_TIME
+    pol = {"continuous": ufoir.SERVE_CONTINUOUS, "one_at_a_time": ufoir.SERVE_ONE_AT_A_TIME,
+           "sjf_one_at_a_time": ufoir.SERVE_SJF_ONE_AT_A_TIME}[policy]
     with ufoir.Server(gpu_ctx, policy=pol, max_active_jobs=8) as srv:
         handles = [srv.submit(d, s) for d, s, _ in jobs]
         for jid, _ in handles:
@@ -140,3 +141,42 @@ def test_injected_allocation_failures_do_not_stop_the_server(ufoir_lib, gpu_ctx,
     for (d, s, kw), (jid, out), rc in zip(jobs, handles, status):
         if rc == ufoir.OK:
             assert np.array_equal(out, _solo(ufoir, gpu_ctx, d, s, kw))
+
+
+def _job_bytes(ufoir, ctx, desc, sino):
+    """Device bytes the server reserves for a job (its peak alone)."""
+    with ufoir.Server(ctx, policy=ufoir.SERVE_ONE_AT_A_TIME) as srv:
+        jid, _ = srv.submit(desc, sino)
+        assert srv.wait(jid, 120000) == ufoir.OK
+        return srv.stats()["peak_hbm_bytes"]
+
+
+@pytest.mark.parametrize("admit_age_ms", [60000, 1])
+def test_admission_passes_a_job_that_does_not_fit_until_it_is_old(ufoir_lib, gpu_ctx, admit_age_ms):
+    # X runs; Y (X's shape) does not fit beside it; Z (small) does. Z may pass
+    # Y while Y is younger than admit_age_ms; once Y is older, nothing passes it.
+    ufoir = ufoir_lib
+    big_n, big_na = 1448, 1200
+    big = ufoir.job_desc(ufoir.METHOD_SIRT, big_n, big_na, float(np.float32(np.pi / big_na)), num_iterations=200)
+    small = ufoir.job_desc(ufoir.METHOD_SIRT, 64, 30, float(np.float32(np.pi / 30)), num_iterations=2)
+    big_sino = np.zeros((big_na, big_n), np.float32)
+    small_sino = np.ones((30, 64), np.float32)
+    bx = _job_bytes(ufoir, gpu_ctx, big, big_sino)
+    bz = _job_bytes(ufoir, gpu_ctx, small, small_sino)
+    budget = bx + bz + (bx // 4)       # X and Z fit together, X and Y do not
+    import time
+    with ufoir.Server(gpu_ctx, hbm_budget=budget, admit_age_ms=admit_age_ms) as srv:
+        x, _ = srv.submit(big, big_sino)
+        y, _ = srv.submit(big, big_sino)
+        time.sleep(0.05)
+        z, _ = srv.submit(small, small_sino)
+        assert srv.wait(z, 120000) == ufoir.OK
+        y_state = srv.poll(y)
+        for jid in (x, y):
+            assert srv.wait(jid, 120000) == ufoir.OK
+        st = srv.stats()
+    assert st["completed"] == 3 and st["peak_hbm_bytes"] <= budget
+    if admit_age_ms > 1000:
+        assert y_state == ufoir.JOB_QUEUED       # Z passed Y while X was running
+    else:
+        assert y_state != ufoir.JOB_QUEUED       # Y was too old to be passed: Z came after it

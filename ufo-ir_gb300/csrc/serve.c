@@ -23,6 +23,7 @@
 
 #define DEFAULT_MAX_ACTIVE 32
 #define DEFAULT_MAX_RUNNING 4
+#define DEFAULT_ADMIT_AGE_MS 2000
 
 enum { PH_QUEUED = 0, PH_RUN = 1, PH_FINAL = 2, PH_END = 3 };
 
@@ -48,6 +49,7 @@ typedef struct job {
     void *graph;
     uint64_t graph_kernels;
     unsigned int done_iters, total_iters;
+    unsigned int total_work_iters;  /* iterations the job asks for (known at submission) */
     double work_per_iter;       /* interpolated samples of one quantum's iteration */
     struct job *next;
 } job;
@@ -91,6 +93,7 @@ void ufoir_serve_config_init(ufoir_serve_config *c)
     c->policy = UFOIR_SERVE_CONTINUOUS;
     c->quantum = 1;
     c->max_running = DEFAULT_MAX_RUNNING;
+    c->admit_age_ms = DEFAULT_ADMIT_AGE_MS;
 }
 
 void ufoir_job_desc_init(ufoir_job_desc *j)
@@ -372,26 +375,85 @@ static void job_finish(ufoir_server *s, job *j, int status)
     pthread_mutex_unlock(&s->mu);
 }
 
+/* Removes j (whose predecessor in the queue is prev, NULL at the head) from
+ * the pending queue. Caller holds the lock. */
+static void unlink_pending(ufoir_server *s, job *prev, job *j)
+{
+    if (prev)
+        prev->next = j->next;
+    else
+        s->pend_head = j->next;
+    if (s->pend_tail == j)
+        s->pend_tail = prev;
+    j->next = NULL;
+}
+
+/* Picks the next queued job to admit, or NULL. Caller holds the lock.
+ *  - ONE_AT_A_TIME: the head of the queue (arrival order), when it fits;
+ *  - SJF_ONE_AT_A_TIME: the queued job with the least total work that fits
+ *    (ties: arrival order);
+ *  - CONTINUOUS: the first job in arrival order that fits the budget. A job
+ *    that does not fit may be passed by later jobs that do, until it has
+ *    waited admit_age_ms; from then on nothing behind it is admitted, so
+ *    the memory that frees up goes to it. */
+static job *pick_admission(ufoir_server *s, double now, job **prev_out)
+{
+    const uint64_t budget = s->cfg.hbm_budget_bytes;
+    job *prev = NULL;
+    if (s->cfg.policy == UFOIR_SERVE_ONE_AT_A_TIME) {
+        job *j = s->pend_head;
+        if (j && s->reserved + j->bytes <= budget) {
+            *prev_out = NULL;
+            return j;
+        }
+        return NULL;
+    }
+    if (s->cfg.policy == UFOIR_SERVE_SJF_ONE_AT_A_TIME) {
+        job *best = NULL, *best_prev = NULL;
+        double best_work = 0.0;
+        for (job *j = s->pend_head; j; prev = j, j = j->next) {
+            if (s->reserved + j->bytes > budget)
+                continue;
+            const double w = j->work_per_iter * (double) j->total_work_iters;
+            if (!best || w < best_work) {
+                best = j;
+                best_prev = prev;
+                best_work = w;
+            }
+        }
+        *prev_out = best_prev;
+        return best;
+    }
+    const double age_limit = 1e-3 * (double) (s->cfg.admit_age_ms ? s->cfg.admit_age_ms : DEFAULT_ADMIT_AGE_MS);
+    for (job *j = s->pend_head; j; prev = j, j = j->next) {
+        if (s->reserved + j->bytes <= budget) {
+            *prev_out = prev;
+            return j;
+        }
+        if (now - j->t_submit >= age_limit)
+            return NULL;      /* an old job waits for memory: admit nothing past it */
+    }
+    return NULL;
+}
+
 static void *worker_main(void *arg)
 {
     ufoir_server *s = (ufoir_server *) arg;
-    const unsigned int max_active =
-        s->cfg.policy == UFOIR_SERVE_ONE_AT_A_TIME ? 1 : (s->cfg.max_active_jobs ? s->cfg.max_active_jobs : DEFAULT_MAX_ACTIVE);
-    const unsigned int max_running =
-        s->cfg.policy == UFOIR_SERVE_ONE_AT_A_TIME ? 1 : (s->cfg.max_running ? s->cfg.max_running : DEFAULT_MAX_RUNNING);
+    const int serial = s->cfg.policy != UFOIR_SERVE_CONTINUOUS;
+    const unsigned int max_active = serial ? 1 : (s->cfg.max_active_jobs ? s->cfg.max_active_jobs : DEFAULT_MAX_ACTIVE);
+    const unsigned int max_running = serial ? 1 : (s->cfg.max_running ? s->cfg.max_running : DEFAULT_MAX_RUNNING);
     for (;;) {
-        /* admission, in arrival order */
+        /* admission (order: see pick_admission) */
         job *admit[64];
         unsigned int n_admit = 0;
         pthread_mutex_lock(&s->mu);
+        const double now = now_s();
         while (s->pend_head && s->n_active + n_admit < max_active && n_admit < 64) {
-            job *j = s->pend_head;
-            if (s->reserved + j->bytes > s->cfg.hbm_budget_bytes)
+            job *prev = NULL;
+            job *j = pick_admission(s, now, &prev);
+            if (!j)
                 break;
-            s->pend_head = j->next;
-            if (!s->pend_head)
-                s->pend_tail = NULL;
-            j->next = NULL;
+            unlink_pending(s, prev, j);
             s->reserved += j->bytes;
             if (s->reserved > s->peak_reserved)
                 s->peak_reserved = s->reserved;
@@ -519,7 +581,8 @@ int ufoir_serve_create(ufoir_ctx *ctx, const ufoir_serve_config *cfg, ufoir_serv
         s->cfg = *cfg;
     else
         ufoir_serve_config_init(&s->cfg);
-    if (s->cfg.policy != UFOIR_SERVE_CONTINUOUS && s->cfg.policy != UFOIR_SERVE_ONE_AT_A_TIME) {
+    if (s->cfg.policy != UFOIR_SERVE_CONTINUOUS && s->cfg.policy != UFOIR_SERVE_ONE_AT_A_TIME &&
+        s->cfg.policy != UFOIR_SERVE_SJF_ONE_AT_A_TIME) {
         free(s);
         return ufoir__fail(ctx, UFOIR_ERR_INVALID, "unknown serve policy %d", cfg->policy);
     }
@@ -577,6 +640,7 @@ int ufoir_serve_submit(ufoir_server *s, const ufoir_job_desc *jd, const float *s
     j->user_vol = vol;
     j->bytes = job_bytes(jd);
     j->work_per_iter = job_work_per_iter(jd);
+    j->total_work_iters = jd->method == UFOIR_METHOD_ASDPOCS ? jd->asdpocs.num_iterations : jd->sart.num_iterations;
     pthread_mutex_lock(&s->mu);
     if (s->stop) {
         pthread_mutex_unlock(&s->mu);
