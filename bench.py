@@ -290,6 +290,7 @@ def run_ufoir(args, dist):
     for _ in range(max(args.warmup, 0)):
         batch.run(1)
     kernel_ms = batch.profile()     # one eager iteration with CUDA events per launch
+    sm_count = ctx.sm_count()
 
     clocks = ClockSampler(dist.local)
     dist.barrier()
@@ -305,6 +306,9 @@ def run_ufoir(args, dist):
     dist.barrier()
     ms_max = dist.max(ms)
     value = S * args.steps * dist.world / (ms_max / 1e3)
+    fast = None
+    if not args.quick and dist.rank == 0:
+        fast = fast_section(ufoir, ctx, batch, d_sino, d_vol, args, sm_count, clock_info)
     batch.close()
 
     e2e, per_job = None, {}
@@ -313,6 +317,9 @@ def run_ufoir(args, dist):
     serve = None
     if not args.quick and not args.no_serve and dist.rank == 0:
         serve = serve_section(ufoir, ctx, args.serve_jobs)
+    mixed = None
+    if not args.quick and dist.rank == 0:
+        mixed = mixed_batch_section(ufoir, ctx)
     methods = methods_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
     models = projector_models_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
 
@@ -358,6 +365,7 @@ def run_ufoir(args, dist):
         "frac": dom_rate / dom_ceiling if dom_ceiling else None,
         "peak_source": "measured in this run: ufoir_sample_ceiling%s (the kernel's own per-sample "
                        "packed-FP32 sequence from shared memory on every SM)" % ("" if dom == "fp" else "_bp")}
+    roofline["fma_pipe_bound"] = fma_pipe_bound(dom, dom_rate, sm_count, clock_info, fast=False)
 
     out = {"metric": METRIC, "value": value, "unit": "slice-iters/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
@@ -375,6 +383,10 @@ def run_ufoir(args, dist):
            **{k: v for k, v in per_job.items() if not k.startswith("_")}}
     if serve is not None:
         out["serve"] = serve
+    if mixed is not None:
+        out["mixed_batch"] = mixed
+    if fast is not None:
+        out["fast_arithmetic"] = fast
     if methods is not None:
         out["methods"] = methods
     if models is not None:
@@ -387,6 +399,72 @@ def run_ufoir(args, dist):
     proj.close()
     ctx.close()
     return out if dist.rank == 0 else None
+
+
+# FP32 operations per pair of samples on the FMA pipe (packed f32x2: one
+# lane-op per sample each), the dominant forms: the BP's coordinate (2),
+# floor (3), interpolation (4: 1 - t, two products, their sum) and sum (1);
+# the FP's inside form: floor (3), interpolation (4), block sum (1) and the
+# coordinate recurrence (1). Fast arithmetic: the BP's shift is folded (1)
+# and interpolation + sum take 3 (T1 - T0, acc + T0, one fma); the FP's
+# interpolation + sum take 3.
+FMA_OPS_PER_SAMPLE = {("bp", False): 10, ("fp", False): 9, ("bp", True): 7, ("fp", True): 7}
+
+
+def fma_pipe_bound(kernel, rate, sm_count, clock_info, fast):
+    """The kernel's sample rate against an FMA-pipe bound independent of its
+    code: SMs x 128 FP32 lanes x the SM clock sampled during the timed
+    region, divided by the FP32 lane-operations one sample needs."""
+    mhz = (clock_info or {}).get("sm_mhz") or 2070.0
+    lane_ops = sm_count * 128 * mhz * 1e6
+    ops = FMA_OPS_PER_SAMPLE[(kernel, fast)]
+    peak = lane_ops / ops
+    return {"kernel": {"fp": "fp_tiles_kernel", "bp": "bp_tiles_kernel"}[kernel], "achieved": rate, "peak": peak,
+            "unit": "samples/s", "frac": rate / peak,
+            "model": f"{sm_count} SMs x 128 FP32 lanes x {mhz:.0f} MHz (sampled) = {lane_ops:.3e} lane-ops/s, "
+                     f"/ {ops} FP32 lane-ops per sample ({'fast' if fast else 'exact'} arithmetic)"}
+
+
+def fast_section(ufoir, ctx, exact_batch, d_sino, d_vol, args, sm_count, clock_info):
+    """The same batched SIRT workload with the projector's fast interpolation
+    arithmetic: slice-iterations/s (CUDA events, the headline's steps), the
+    per-kernel times and sample rates with their FMA-pipe bound, and the
+    relative L2 distance of 10 iterations from the exact path's (which equals
+    the reference arithmetic bit for bit)."""
+    n, na, S = N_DETS, N_ANGLES, args.slices
+    step = float(np.float32(np.pi / na))
+    projf = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=0, arithmetic=ufoir.ARITH_FAST)
+    d_vol_f = ufoir.DeviceArray(ctx, (S, n, n), zero=True)
+    fb = ufoir.SirtBatch(projf, d_sino, d_vol_f, relaxation_factor=RELAX)
+    for _ in range(max(args.warmup, 0)):
+        fb.run(1)
+    kms = fb.profile()
+    ctx.synchronize()
+    ctx.timer_begin()
+    for _ in range(args.steps):
+        fb.run(1)
+    ms = ctx.timer_end()
+    fp_samples = S * na * n * math.ceil(n / 64) * 64
+    bp_samples = S * n * n * na
+    fp_rate = fp_samples / (kms["fp"] / 1e3)
+    bp_rate = bp_samples / (kms["bp"] / 1e3)
+    fb.reset()
+    fb.run(10)
+    exact_batch.reset()
+    exact_batch.run(10)
+    a = d_vol_f.slice(0).download().astype(np.float64)
+    b = d_vol.slice(0).download().astype(np.float64)
+    out = {"value": S * args.steps / (ms / 1e3), "unit": "slice-iters/s", "ms_per_step": ms / args.steps,
+           "kernel_ms": kms, "fp_samples_per_s": fp_rate, "bp_samples_per_s": bp_rate,
+           "fma_pipe_bound_bp": fma_pipe_bound("bp", bp_rate, sm_count, clock_info, fast=True),
+           "fma_pipe_bound_fp": fma_pipe_bound("fp", fp_rate, sm_count, clock_info, fast=True),
+           "rel_l2_vs_exact_10_iterations_slice0": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+           "what": "projector arithmetic \"fast\": T0 + t (T1 - T0) fused into the sum, BP shift folded; "
+                   "the headline value above uses the exact (reference) arithmetic"}
+    fb.close()
+    d_vol_f.close()
+    projf.close()
+    return out
 
 
 def end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S):
@@ -507,6 +585,97 @@ def serve_section(ufoir, ctx, n_jobs):
         st = run_serve(ufoir, ctx, jobs, pol)
         out[name] = {k: st[k] for k in keys if k in st}
         out[name]["samples_per_s"] = samples / st["busy_seconds"] if st.get("busy_seconds") else None
+    return out
+
+
+# mixed batch: SIRT jobs of the serve sizes and angle counts
+MIX_JOBS = 16
+MIX_ITERS = 20
+MIX_SEED = 6006
+
+
+def mixed_batch_section(ufoir, ctx):
+    """A mix of one-slice SIRT jobs of uneven size (grid n in {367, 724, 1448,
+    2900}, angles U{90..1800}, seeded), each advanced MIX_ITERS iterations,
+    all data resident in HBM, three ways on the same GPU:
+      per_job_process  ufoir_sirt_process per job (weights, capture and
+                       iterations inside each call: the plain per-job path);
+      per_job_resident one resident ufoir_sirt_batch per job, set up before
+                       the timer, run one job after another;
+      mixed_batch      one ufoir_batch of all jobs, set up before the timer
+                       (and the same with the autotuner choosing the forward
+                       projector's launch shapes).
+    Rates are slice-iterations/s and interpolated samples/s (2 n^2 n_a per
+    iteration); each member's result equals its per-job result bit for bit
+    (tests/test_gpu_batch.py)."""
+    from ufoir import synth
+    rng = np.random.default_rng(MIX_SEED)
+    jobs, cache = [], {}
+    for i in range(MIX_JOBS):
+        P, n = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
+        na = int(rng.integers(90, 1801))
+        step = float(np.float32(np.pi / na))
+        if n not in cache:
+            cache[n] = synth.ellipse_phantom(n, P, 10, seed=MIX_SEED + n)
+        proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=1)
+        clean = proj.forward(cache[n], np.zeros((na, n), np.float32))
+        proj.close()
+        sino, _ = synth.poisson_noise(clean, I0, seed=MIX_SEED + i)
+        jobs.append((n, na, step, ufoir.DeviceArray.from_numpy(ctx, sino), ufoir.DeviceArray(ctx, (n, n), zero=True)))
+    samples = float(sum(2.0 * n * n * na for n, na, *_ in jobs)) * MIX_ITERS
+    slice_iters = MIX_JOBS * MIX_ITERS
+    out = {"workload": f"{MIX_JOBS} one-slice SIRT jobs, grid n in {{367,724,1448,2900}}, angles U{{90..1800}} "
+                       f"(seed {MIX_SEED}), {MIX_ITERS} iterations each, data resident in HBM",
+           "jobs": [[n, na] for n, na, *_ in jobs], "samples": samples}
+
+    def rate(sec):
+        return {"seconds": sec, "slice_iters_per_s": slice_iters / sec, "samples_per_s": samples / sec}
+
+    projs = [ufoir.ParallelProjector(ctx, step=st, angles_num=na, is_forward=0) for n, na, st, *_ in jobs]
+    # per-job process calls (one warm pass of one iteration each first)
+    for pj, (n, na, st, ds, dv) in zip(projs, jobs):
+        ufoir.sirt(pj, ds, dv, num_iterations=1)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for pj, (n, na, st, ds, dv) in zip(projs, jobs):
+        ufoir.sirt(pj, ds, dv, num_iterations=MIX_ITERS)
+    ctx.synchronize()
+    out["per_job_process"] = rate(time.perf_counter() - t0)
+    # per-job resident batches
+    sb = [ufoir.SirtBatch(pj, ds, dv, relaxation_factor=RELAX) for pj, (n, na, st, ds, dv) in zip(projs, jobs)]
+    for b in sb:
+        b.run(1)
+    ctx.synchronize()
+    ctx.timer_begin()
+    for b in sb:
+        b.run(MIX_ITERS)
+    out["per_job_resident"] = rate(ctx.timer_end() / 1e3)
+    for b in sb:
+        b.close()
+    # the mixed batch, fixed rules and autotuned
+    for name, tune in (("mixed_batch", False), ("mixed_batch_autotuned", True)):
+        ctx.set_autotune(tune)
+        t0 = time.perf_counter()
+        b = ufoir.Batch(ctx, [(ds, dv, dict(step=st, relaxation_factor=RELAX)) for n, na, st, ds, dv in jobs])
+        setup_s = time.perf_counter() - t0
+        b.run(1)
+        ctx.synchronize()
+        ctx.timer_begin()
+        b.run(MIX_ITERS)
+        r = rate(ctx.timer_end() / 1e3)
+        r["setup_seconds"] = setup_s
+        r["launches_per_iteration"], r["fp_launch_shapes"] = b.launches()
+        b.close()
+        out[name] = r
+    ctx.set_autotune(False)
+    out["speedup_vs_per_job_resident"] = out["mixed_batch"]["slice_iters_per_s"] / out["per_job_resident"]["slice_iters_per_s"]
+    out["speedup_autotuned_vs_per_job_resident"] = (out["mixed_batch_autotuned"]["slice_iters_per_s"] /
+                                                    out["per_job_resident"]["slice_iters_per_s"])
+    for pj in projs:
+        pj.close()
+    for n, na, st, ds, dv in jobs:
+        ds.close()
+        dv.close()
     return out
 
 
@@ -641,11 +810,19 @@ def main():
                     help="also time one call of each other configured method workload (C1, C2, C3a/b, C4)")
     ap.add_argument("--projector-models", action="store_true",
                     help="only time the Joseph and Siddon projectors on one resident 1448^2 x 1200 slice")
+    ap.add_argument("--mixed-batch", action="store_true",
+                    help="only the mixed-batch comparison (per-job vs one batch of uneven SIRT jobs)")
     args = ap.parse_args()
     if args.projector_models:
         import ufoir
         ctx = ufoir.Context(int(os.environ.get("LOCAL_RANK", "0")))
         print(json.dumps(projector_models_section(ufoir, ctx)), flush=True)
+        ctx.close()
+        return
+    if args.mixed_batch:
+        import ufoir
+        ctx = ufoir.Context(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(mixed_batch_section(ufoir, ctx)), flush=True)
         ctx.close()
         return
     dist = Dist()

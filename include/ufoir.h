@@ -95,6 +95,8 @@ UFOIR_API int ufoir_host_alloc(ufoir_ctx *ctx, size_t bytes, void **ptr);
 UFOIR_API int ufoir_host_free(ufoir_ctx *ctx, void *ptr);
 /* Copy between any combination of host and device memory; synchronous. */
 UFOIR_API int ufoir_memcpy(ufoir_ctx *ctx, void *dst, const void *src, size_t bytes);
+/* Streaming multiprocessors of the context's GPU. */
+UFOIR_API int ufoir_ctx_sm_count(const ufoir_ctx *ctx);
 /* Number of kernels this library launched on the context so far. */
 UFOIR_API uint64_t ufoir_ctx_kernel_launches(const ufoir_ctx *ctx);
 /* CUDA-event timer on the context's stream: begin records a start event,
@@ -145,7 +147,23 @@ typedef struct {
     float step;
     float relaxation;
     float correction_scale;
+    int arithmetic;        /* extension, no reference counterpart: UFOIR_ARITH_EXACT (default) or
+                              UFOIR_ARITH_FAST, see below ["arithmetic": "exact" | "fast"] */
 } ufoir_projector_params;
+
+/* Interpolation arithmetic of the tiled Joseph projectors (forward over many
+ * angles, backprojection over 16 or more angles).
+ * EXACT: every operation rounds as the reference's kernels do
+ *        ((1 - t) T0 + t T1, products unfused), so results equal the
+ *        reference's bit for bit.
+ * FAST:  T0 + t (T1 - T0) with the product fused into the accumulation, and
+ *        the backprojector's detector shift folded into its row terms: about
+ *        a third fewer floating-point operations per sample. Results differ
+ *        from the reference's in the last bits: relative L2 below 1e-5 after
+ *        one projection and below 1e-4 after 100 SIRT iterations (the
+ *        tolerance of this path), tested. The per-angle SART kernels and the
+ *        few-angle kernels always compute exactly. */
+enum { UFOIR_ARITH_EXACT = 0, UFOIR_ARITH_FAST = 1 };
 
 typedef struct ufoir_projector ufoir_projector;
 
@@ -316,6 +334,71 @@ UFOIR_API int ufoir_sirt_batch_profile(ufoir_sirt_batch *b, float ms[3]);
 UFOIR_API void ufoir_sirt_batch_destroy(ufoir_sirt_batch *b);
 
 /* ------------------------------------------------------------------------ */
+/* Autotuner of the tiled forward projector (no reference counterpart; the  */
+/* reference's OpenCL launches use fixed work sizes,                        */
+/* src/tasks/ufo-ir-parallel-projector-task.c:501-625). With autotune on, a */
+/* context searches the forward projector's launch shapes (angles per tile, */
+/* detector pairs per thread, rows per staged chunk, CTAs per tile, column  */
+/* windows) the first time a method or batch meets a geometry (n_dets,      */
+/* n_angles, step, axis) and slice count, timing each candidate with CUDA   */
+/* events on scratch data, and keeps the fastest (the fixed rules unless a  */
+/* shape is at least 2 % faster). Every shape computes each ray with the    */
+/* same arithmetic, so results do not depend on the choice, bit for bit.    */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int J, A, win, K, dsplit, threads;   /* the chosen shape */
+    int tuned;                           /* 1 if the search ran (or was cached), 0 = fixed rules */
+    unsigned int candidates;             /* shapes timed */
+    float ms_default, ms_tuned;          /* one forward projection, fixed rules vs chosen shape */
+} ufoir_fp_tuning;
+
+/* on = 1: search shapes (default 0: the fixed rules). */
+UFOIR_API int ufoir_ctx_set_autotune(ufoir_ctx *ctx, int on);
+/* Searches now for the projector's geometry (set by a requisition or a
+ * forward/backward call) and n_slices slices, even with autotune off, and
+ * reports the result; later calls on this projector with n_slices slices use
+ * the chosen shape. */
+UFOIR_API int ufoir_projector_autotune(ufoir_projector *proj, size_t n_slices, ufoir_fp_tuning *out);
+
+/* ------------------------------------------------------------------------ */
+/* Mixed SIRT batches: many one-slice SIRT jobs of different sizes and       */
+/* angle counts advanced together. One iteration of every member is a fixed */
+/* small set of launches captured in one CUDA graph: one padding launch for */
+/* all members, one forward-projection launch per distinct launch shape (the */
+/* autotuner's per geometry when the context's autotune is on), and one     */
+/* backprojection launch for all members; each launch walks a work list of  */
+/* (member, tile) items, biggest members first. Each member computes        */
+/* exactly what ufoir_sirt_process computes for it alone, bit for bit. The  */
+/* reference advances one slice per process() call                         */
+/* (src/core/ufo-ir-method-task.c:221-252, src/tasks/ufo-ir-sirt-task.c:164-222). */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    unsigned int n_dets, n_angles;    /* sinogram dims; the volume is n_dets x n_dets */
+    float step;                       /* projector "step" (radians) */
+    float axis_position;              /* projector "axis_position" (-1 = n_dets / 2) */
+    float relaxation_factor;          /* SIRT "relaxation_factor" [0, 1] */
+    const float *sino;                /* device memory, n_angles x n_dets */
+    float *vol;                       /* device memory, n_dets x n_dets */
+    int keep_vol;                     /* 0: start from x = 0 (as process() does); 1: from vol's content */
+    int arithmetic;                   /* UFOIR_ARITH_EXACT (0) or UFOIR_ARITH_FAST */
+} ufoir_batch_job;
+
+typedef struct ufoir_batch ufoir_batch;
+
+/* Members need n_angles >= 16 and an axis at least half a pixel inside the
+ * image (the tiled projectors; others give UFOIR_ERR_UNSUPPORTED). sino and
+ * vol must stay valid until destroy. */
+UFOIR_API int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_jobs, ufoir_batch **out);
+/* Advances every active member by `iterations` SIRT iterations (synchronous). */
+UFOIR_API int ufoir_batch_run(ufoir_batch *b, unsigned int iterations);
+/* Freezes (0) or resumes (1) a member; frozen members are skipped by every
+ * launch. All members start active. */
+UFOIR_API int ufoir_batch_set_active(ufoir_batch *b, size_t member, int active);
+/* Kernel launches of one batched iteration, and distinct forward shapes. */
+UFOIR_API int ufoir_batch_launches(const ufoir_batch *b, unsigned int *launches, unsigned int *fp_shapes);
+UFOIR_API void ufoir_batch_destroy(ufoir_batch *b);
+
+/* ------------------------------------------------------------------------ */
 /* Serving: a request loop over reconstruction jobs of mixed size, method   */
 /* and iteration count. The reference processes one slice per process()    */
 /* call on a ufo-core GPU node thread (src/core/ufo-ir-method-task.c:221-252) */
@@ -367,6 +450,9 @@ typedef struct {
                                          with the least remaining work first; 0 = 4 */
     unsigned int admit_age_ms;        /* CONTINUOUS: how long a queued job that does not fit the
                                          budget may be passed by later jobs; 0 = 2000 */
+    unsigned int batch_sirt;          /* CONTINUOUS: 1 (default) = the SIRT jobs the tiled projectors
+                                         serve advance together, one mixed batch (ufoir_batch) of
+                                         the idle ones per quantum; 0 = each on its own graph */
 } ufoir_serve_config;
 
 typedef struct {
@@ -377,6 +463,7 @@ typedef struct {
     double busy_seconds;              /* first submission to last completion */
     uint64_t peak_hbm_bytes;          /* largest sum of reserved job memory */
     unsigned int peak_active_jobs;
+    uint64_t batched_iterations;      /* mixed-batch iterations issued (batch_sirt) */
 } ufoir_serve_stats;
 
 typedef struct ufoir_server ufoir_server;

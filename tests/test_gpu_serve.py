@@ -44,13 +44,13 @@ def _solo(ufoir, ctx, desc, sino, kw):
     return out
 
 
-@pytest.mark.parametrize("policy", ["continuous", "one_at_a_time", "sjf_one_at_a_time"])
+@pytest.mark.parametrize("policy", ["continuous", "continuous_unbatched", "one_at_a_time", "sjf_one_at_a_time"])
 def test_results_in_the_mix_equal_results_alone(ufoir_lib, gpu_ctx, oracle, policy):
     ufoir = ufoir_lib
     jobs = _jobs(ufoir, oracle)
-    pol = {"continuous": ufoir.SERVE_CONTINUOUS, "one_at_a_time": ufoir.SERVE_ONE_AT_A_TIME,
-           "sjf_one_at_a_time": ufoir.SERVE_SJF_ONE_AT_A_TIME}[policy]
-    with ufoir.Server(gpu_ctx, policy=pol, max_active_jobs=8) as srv:
+    pol = {"continuous": ufoir.SERVE_CONTINUOUS, "continuous_unbatched": ufoir.SERVE_CONTINUOUS,
+           "one_at_a_time": ufoir.SERVE_ONE_AT_A_TIME, "sjf_one_at_a_time": ufoir.SERVE_SJF_ONE_AT_A_TIME}[policy]
+    with ufoir.Server(gpu_ctx, policy=pol, max_active_jobs=8, batch_sirt=policy == "continuous") as srv:
         handles = [srv.submit(d, s) for d, s, _ in jobs]
         for jid, _ in handles:
             assert srv.wait(jid, 120000) == ufoir.OK
@@ -60,8 +60,11 @@ def test_results_in_the_mix_equal_results_alone(ufoir_lib, gpu_ctx, oracle, poli
     assert st["p99_latency_ms"] >= st["p50_latency_ms"] > 0
     if policy == "continuous":
         assert st["peak_active_jobs"] >= 2
+        assert st["batched_iterations"] > 0       # the SIRT jobs advanced in the mixed batch
+    elif policy == "continuous_unbatched":
+        assert st["peak_active_jobs"] >= 2 and st["batched_iterations"] == 0
     else:
-        assert st["peak_active_jobs"] == 1
+        assert st["peak_active_jobs"] == 1 and st["batched_iterations"] == 0
     for (d, s, kw), (_, out) in zip(jobs, handles):
         alone = _solo(ufoir, gpu_ctx, d, s, kw)
         assert np.array_equal(out, alone), (d.method, d.n_dets, float(np.abs(out - alone).max()))

@@ -51,8 +51,22 @@ void ufoir_ctx_destroy(ufoir_ctx *ctx)
 {
     if (!ctx)
         return;
+    ufoir__tune_free(ctx);
     udev_destroy(ctx->dev);
     free(ctx);
+}
+
+int ufoir_ctx_sm_count(const ufoir_ctx *ctx)
+{
+    return ctx ? udev_sm_count(ctx->dev) : 0;
+}
+
+int ufoir_ctx_set_autotune(ufoir_ctx *ctx, int on)
+{
+    if (!ctx || (on != 0 && on != 1))
+        return UFOIR_ERR_INVALID;
+    ctx->autotune = on;
+    return UFOIR_OK;
 }
 
 const char *ufoir_last_error(const ufoir_ctx *ctx)

@@ -145,7 +145,15 @@ static int parse_projector(gctx *g, const json_value *n, ufoir_projector_params 
             rc = get_float(g, name, k, v, -FLT_MAX, FLT_MAX, &p->relaxation);
         else if (name_is(k, "correction-scale"))
             rc = get_float(g, name, k, v, -FLT_MAX, FLT_MAX, &p->correction_scale);
-        else
+        else if (name_is(k, "arithmetic")) {
+            /* extension: the tiled projectors' interpolation arithmetic */
+            if (v->type == JSON_STRING && strcmp(v->string, "exact") == 0)
+                p->arithmetic = UFOIR_ARITH_EXACT;
+            else if (v->type == JSON_STRING && strcmp(v->string, "fast") == 0)
+                p->arithmetic = UFOIR_ARITH_FAST;
+            else
+                rc = gfail(g, UFOIR_ERR_INVALID, "%s: \"arithmetic\" must be \"exact\" or \"fast\"", name);
+        } else
             rc = gfail(g, UFOIR_ERR_INVALID, "%s: no property \"%s\"", name, k);
     }
     return rc;

@@ -10,10 +10,15 @@
 #include "udev.h"
 #include "ufoir.h"
 
+struct ufoir__tune_entry;
+
 struct ufoir_ctx {
     udev *dev;
     uint64_t hbm_budget;
     char create_err[256];
+    int autotune;                       /* 1: forward-projector launch shapes are searched per geometry */
+    struct ufoir__tune_entry *tune;     /* cache of searched shapes (autotune.c) */
+    int n_tune, cap_tune;
 };
 
 struct ufoir_projector {
@@ -31,12 +36,16 @@ struct ufoir_projector {
     float *d_sin, *d_cos;
     unsigned char *d_dir;
     unsigned int lut_cap;
-    /* angle tiles of the tiled forward projector (int4 each, device) */
-    void *d_tiles;
-    int n_tiles;
-    int tiles_A;
-    int tiles_valid;
-    float tiles_spread;         /* max over tiles of the angles' coordinate spread (columns) */
+    /* angle tiles of the tiled forward projector, one list per tile width
+     * A = 1, 2, 4, 8 (slot 0..3; int4 each, device) */
+    void *d_tiles[4];
+    int n_tiles[4];
+    int tiles_valid[4];
+    float tiles_spread[4];      /* max over tiles of the angles' coordinate spread (columns) */
+    /* launch shape chosen by the autotuner for fp_cfg_slices slices */
+    int fp_cfg_valid;
+    int fp_cfg_slices;
+    udev_fp_cfg fp_cfg;
 };
 
 /* Scratch of the tiled forward projector: the padded copy and the padded
@@ -116,6 +125,39 @@ int ufoir__asd_setup(ufoir__asd_state *s, ufoir_projector *proj, const ufoir_asd
 int ufoir__asd_outer(ufoir__asd_state *s);
 void ufoir__asd_release(ufoir__asd_state *s);
 size_t ufoir__asd_bytes(size_t n, size_t na, size_t S);
+
+/* The angle tiles of width A (1, 2, 4 or 8) of the prepared geometry,
+ * built on first use (not inside a stream capture). */
+int ufoir__projector_tiles(ufoir_projector *p, int A, const void **d_tiles, int *n_tiles, float *spread);
+/* The launch shape of the tiled forward projector for n_slices slices: the
+ * tuned one where the autotuner has searched this geometry and slice count
+ * (its tiles are built then), else the fixed rules. UFOIR_ERR_UNSUPPORTED if
+ * the tiled kernel cannot serve the size. */
+int ufoir__fp_shape(ufoir_projector *p, int n_slices, udev_fp_cfg *c, const void **d_tiles, int *n_tiles);
+/* Autotuner (autotune.c): with the context's autotune on, searches the
+ * launch shapes for this geometry and n_slices (once per context; cached)
+ * and records the fastest on the projector. A no-op when autotune is off.
+ * Must not run inside a stream capture. */
+int ufoir__fp_tune(ufoir_projector *p, int n_slices, ufoir_fp_tuning *out);
+void ufoir__tune_free(ufoir_ctx *ctx);
+
+/* A member of a mixed SIRT batch whose buffers its owner keeps (the serve
+ * loop): prepared projector (tiles built), sinogram b, iterate x, weights R
+ * and C, residual and padded-copy scratch (P, TP: zero pad columns), and the
+ * slice count its forward launch shape is chosen for. */
+typedef struct {
+    ufoir_projector *p;
+    const float *b;
+    float *x, *R, *C, *resid, *P, *TP;
+    float lambda;
+    int shape_slices;
+} ufoir__bmember;
+/* Work lists and the captured iteration for these members (batch.c); the
+ * batch owns none of the members' buffers. Not inside a stream capture. */
+int ufoir__batch_build(ufoir_ctx *ctx, const ufoir__bmember *members, int n, ufoir_batch **out);
+/* Enqueues `iterations` iterations of every active member on the current
+ * stream, without waiting. */
+int ufoir__batch_launch(ufoir_batch *b, unsigned int iterations);
 
 /* The two launches of ufoir__fp_full, separately (for timing). */
 int ufoir__fp_prepare(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol, int n_slices);

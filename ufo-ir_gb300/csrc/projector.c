@@ -24,6 +24,7 @@ void ufoir_projector_params_init(ufoir_projector_params *p)
     p->step = 0.0f;                  /* :108 */
     p->relaxation = 1.0f;            /* :109 */
     p->correction_scale = 1.0f;      /* :110 */
+    p->arithmetic = UFOIR_ARITH_EXACT;
 }
 
 static int check_params(ufoir_ctx *ctx, ufoir_projector_params *p)
@@ -48,6 +49,8 @@ static int check_params(ufoir_ctx *ctx, ufoir_projector_params *p)
         return ufoir__fail(ctx, UFOIR_ERR_INVALID, "step %g outside [0, MAX]", (double) p->step);
     if (!isfinite(p->relaxation) || !isfinite(p->correction_scale))
         return ufoir__fail(ctx, UFOIR_ERR_INVALID, "relaxation/correction_scale must be finite");
+    if (p->arithmetic != UFOIR_ARITH_EXACT && p->arithmetic != UFOIR_ARITH_FAST)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "arithmetic %d is neither exact (0) nor fast (1)", p->arithmetic);
     return UFOIR_OK;
 }
 
@@ -88,12 +91,15 @@ static void free_geometry(ufoir_projector *p)
         udev_free(p->ctx->dev, p->d_cos);
     if (p->d_dir)
         udev_free(p->ctx->dev, p->d_dir);
-    if (p->d_tiles)
-        udev_free(p->ctx->dev, p->d_tiles);
+    for (int k = 0; k < 4; k++) {
+        if (p->d_tiles[k])
+            udev_free(p->ctx->dev, p->d_tiles[k]);
+        p->d_tiles[k] = NULL;
+        p->tiles_valid[k] = 0;
+    }
+    p->fp_cfg_valid = 0;
     p->d_sin = p->d_cos = NULL;
     p->d_dir = NULL;
-    p->d_tiles = NULL;
-    p->tiles_valid = 0;
     p->lut_cap = 0;
     p->have_geometry = 0;
 }
@@ -202,7 +208,9 @@ static int build_geometry(ufoir_projector *p, unsigned int n_angles)
     p->n_angles = n_angles;
     p->lut_step = step;
     p->have_geometry = 1;
-    p->tiles_valid = 0;
+    for (int k = 0; k < 4; k++)
+        p->tiles_valid[k] = 0;
+    p->fp_cfg_valid = 0;
     return UFOIR_OK;
 }
 
@@ -241,6 +249,7 @@ void ufoir__projector_geom(const ufoir_projector *p, udev_geom *g)
     g->d_sin = p->d_sin;
     g->d_cos = p->d_cos;
     g->d_dir = p->d_dir;
+    g->fast_arith = p->prm.arithmetic == UFOIR_ARITH_FAST;
 }
 
 int ufoir_projector_get_requisition(ufoir_projector *proj, const size_t in_dims[2], size_t out_dims[2])
@@ -306,52 +315,80 @@ static double tile_spread(const ufoir_projector *p, unsigned int first, unsigned
     return spread;
 }
 
+static int tile_slot(int A)
+{
+    return A == 1 ? 0 : A == 2 ? 1 : A == 4 ? 2 : A == 8 ? 3 : -1;
+}
+
 /* Angle tiles of the tiled forward projector: runs of at most A angles that
  * never cross a direction boundary (the full subsets, cut into pieces). */
-static int ensure_tiles(ufoir_projector *p)
+int ufoir__projector_tiles(ufoir_projector *p, int A, const void **d_tiles, int *n_tiles, float *spread_out)
 {
     ufoir_ctx *ctx = p->ctx;
-    const int A = udev_fp_tile_angles(ctx->dev, (int) p->n_dets);
-    if (A <= 0)
-        return UFOIR_ERR_UNSUPPORTED;
-    if (p->tiles_valid && p->tiles_A == A)
-        return UFOIR_OK;
-    int count = 0;
-    for (unsigned int i = 0; i < p->n_subsets; i++)
-        count += (int) ((p->subsets[i].n + (unsigned int) A - 1) / (unsigned int) A);
-    int *h = (int *) malloc(sizeof(int) * 4 * (size_t) (count ? count : 1));
-    if (!h)
-        return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
-    int t = 0;
+    const int k = tile_slot(A);
+    if (k < 0)
+        return ufoir__fail(ctx, UFOIR_ERR_INVALID, "tile width %d", A);
+    if (!p->tiles_valid[k]) {
+        int count = 0;
+        for (unsigned int i = 0; i < p->n_subsets; i++)
+            count += (int) ((p->subsets[i].n + (unsigned int) A - 1) / (unsigned int) A);
+        int *h = (int *) malloc(sizeof(int) * 4 * (size_t) (count ? count : 1));
+        if (!h)
+            return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+        int t = 0;
+        udev_geom g;
+        ufoir__projector_geom(p, &g);
+        double spread = 0.0;
+        for (unsigned int i = 0; i < p->n_subsets; i++)
+            for (unsigned int a = 0; a < p->subsets[i].n; a += (unsigned int) A, t++) {
+                const unsigned int left = p->subsets[i].n - a;
+                h[4 * t + 0] = (int) (p->subsets[i].offset + a);
+                h[4 * t + 1] = (int) (left < (unsigned int) A ? left : (unsigned int) A);
+                h[4 * t + 2] = p->subsets[i].direction;
+                h[4 * t + 3] = 0;
+                const double sp = tile_spread(p, (unsigned int) h[4 * t + 0], (unsigned int) h[4 * t + 1],
+                                              p->subsets[i].direction, (double) g.axis);
+                spread = sp > spread ? sp : spread;
+            }
+        if (p->d_tiles[k])
+            udev_free(ctx->dev, p->d_tiles[k]);
+        p->d_tiles[k] = NULL;
+        int rc = udev_malloc(ctx->dev, &p->d_tiles[k], sizeof(int) * 4 * (size_t) (count ? count : 1));
+        if (!rc)
+            rc = udev_memcpy(ctx->dev, p->d_tiles[k], h, sizeof(int) * 4 * (size_t) count);
+        free(h);
+        if (rc)
+            return rc;
+        p->n_tiles[k] = count;
+        p->tiles_spread[k] = (float) spread;
+        p->tiles_valid[k] = 1;
+    }
+    if (d_tiles)
+        *d_tiles = p->d_tiles[k];
+    if (n_tiles)
+        *n_tiles = p->n_tiles[k];
+    if (spread_out)
+        *spread_out = p->tiles_spread[k];
+    return UFOIR_OK;
+}
+
+int ufoir__fp_shape(ufoir_projector *p, int n_slices, udev_fp_cfg *c, const void **d_tiles, int *n_tiles)
+{
+    udev *d = p->ctx->dev;
     udev_geom g;
     ufoir__projector_geom(p, &g);
-    double spread = 0.0;
-    for (unsigned int i = 0; i < p->n_subsets; i++)
-        for (unsigned int a = 0; a < p->subsets[i].n; a += (unsigned int) A, t++) {
-            const unsigned int left = p->subsets[i].n - a;
-            h[4 * t + 0] = (int) (p->subsets[i].offset + a);
-            h[4 * t + 1] = (int) (left < (unsigned int) A ? left : (unsigned int) A);
-            h[4 * t + 2] = p->subsets[i].direction;
-            h[4 * t + 3] = 0;
-            const double sp = tile_spread(p, (unsigned int) h[4 * t + 0], (unsigned int) h[4 * t + 1],
-                                          p->subsets[i].direction, (double) g.axis);
-            spread = sp > spread ? sp : spread;
-        }
-    p->tiles_spread = (float) spread;
-    if (p->d_tiles)
-        udev_free(ctx->dev, p->d_tiles);
-    p->d_tiles = NULL;
-    p->tiles_valid = 0;
-    int rc = udev_malloc(ctx->dev, &p->d_tiles, sizeof(int) * 4 * (size_t) (count ? count : 1));
-    if (!rc)
-        rc = udev_memcpy(ctx->dev, p->d_tiles, h, sizeof(int) * 4 * (size_t) count);
-    free(h);
+    if (p->fp_cfg_valid && p->fp_cfg_slices == n_slices) {
+        *c = p->fp_cfg;
+        return ufoir__projector_tiles(p, c->A, d_tiles, n_tiles, NULL);
+    }
+    const int A = udev_fp_tile_angles(d, (int) p->n_dets);
+    if (A <= 0)
+        return UFOIR_ERR_UNSUPPORTED;
+    float spread = 0.0f;
+    int rc = ufoir__projector_tiles(p, A, d_tiles, n_tiles, &spread);
     if (rc)
         return rc;
-    p->n_tiles = count;
-    p->tiles_A = A;
-    p->tiles_valid = 1;
-    return UFOIR_OK;
+    return udev_fp_default_cfg(d, &g, *n_tiles, n_slices, spread, c);
 }
 
 int ufoir__fp_scratch_alloc(ufoir_projector *p, ufoir_fp_scratch *s, size_t slices)
@@ -392,10 +429,13 @@ int ufoir__fp_project(ufoir_projector *p, ufoir_fp_scratch *s, const float *vol,
 {
     udev_geom g;
     ufoir__projector_geom(p, &g);
-    const int rc = ensure_tiles(p);
+    udev_fp_cfg c;
+    const void *tiles = NULL;
+    int n_tiles = 0;
+    const int rc = ufoir__fp_shape(p, n_slices, &c, &tiles, &n_tiles);
     if (rc == UFOIR_OK)
-        return udev_fp_tiles(p->ctx->dev, &g, p->d_tiles, p->n_tiles, p->tiles_spread, s->P, s->TP, src, w, w_shared,
-                             out, scale, n_slices);
+        return udev_fp_tiles_cfg(p->ctx->dev, &g, &c, tiles, n_tiles, s->P, s->TP, src, w, w_shared, out, scale,
+                                 n_slices);
     if (rc != UFOIR_ERR_UNSUPPORTED)
         return rc;
     return udev_fp(p->ctx->dev, &g, 0, (int) p->n_angles, -1, vol, s->TP, src, w, w_shared, out, scale, n_slices);

@@ -50,6 +50,7 @@ typedef struct job {
     uint64_t graph_kernels;
     unsigned int done_iters, total_iters;
     unsigned int total_work_iters;  /* iterations the job asks for (known at submission) */
+    int pooled;                 /* SIRT job that advances in the server's mixed batch */
     double work_per_iter;       /* interpolated samples of one quantum's iteration */
     struct job *next;
 } job;
@@ -75,6 +76,14 @@ struct ufoir_server {
     size_t n_lat, cap_lat;
     double first_submit, last_done;
     uint64_t starts;            /* job set-ups attempted (failure injection) */
+    /* CONTINUOUS: SIRT jobs advance together, one mixed batch (batch.c) of
+     * the idle ones per quantum, on the pool's own stream */
+    void *pool_stream;
+    ufoir_batch *pool;
+    uint64_t *pool_ids;         /* job ids of the built batch, in member order */
+    unsigned int n_pool, cap_pool;
+    int pool_off;               /* set if a batch could not be built: per-job graphs from then on */
+    uint64_t pool_quanta;       /* batched iterations issued (statistics) */
 };
 
 static double now_s(void)
@@ -94,6 +103,7 @@ void ufoir_serve_config_init(ufoir_serve_config *c)
     c->quantum = 1;
     c->max_running = DEFAULT_MAX_RUNNING;
     c->admit_age_ms = DEFAULT_ADMIT_AGE_MS;
+    c->batch_sirt = 1;
 }
 
 void ufoir_job_desc_init(ufoir_job_desc *j)
@@ -207,6 +217,18 @@ static int capture_body(ufoir_server *s, job *j, int (*body)(void *), void *arg)
     return UFOIR_OK;
 }
 
+/* A SIRT job the mixed batch can carry: the tiled projectors serve its
+ * geometry (at least 16 angles, at most 16 direction runs, clamp edges in
+ * order, a tiled forward launch shape). */
+static int pool_eligible(ufoir_server *s, ufoir_projector *p)
+{
+    if (p->n_angles < 16 || p->n_subsets > 16 || udev_fp_tile_angles(s->ctx->dev, (int) p->n_dets) <= 0)
+        return 0;
+    const float n = (float) p->n_dets, axis = ufoir__axis(p);
+    const float half = n - axis * 2.0f < 0.0f ? n - axis : axis;
+    return axis - half + 0.5f <= axis + half - 0.5f;
+}
+
 /* Set-up on the job's stream: upload, weights, captured iteration. */
 static int job_start(ufoir_server *s, job *j)
 {
@@ -260,6 +282,8 @@ static int job_start(ufoir_server *s, job *j)
         if ((rc = capture_body(s, j, ufoir__sirt_body, &j->sirt)))
             return rc;
         j->total_iters = jd->sart.num_iterations;
+        j->pooled = s->cfg.policy == UFOIR_SERVE_CONTINUOUS && s->cfg.batch_sirt && !s->pool_off &&
+                    pool_eligible(s, p);
         break;
     case UFOIR_METHOD_SART:
         if ((rc = ufoir__alloc(ctx, &j->R, ns)) || (rc = ufoir__alloc(ctx, &j->resid, ns > nv ? ns : nv)) ||
@@ -373,6 +397,87 @@ static void job_finish(ufoir_server *s, job *j, int status)
         }
     pthread_cond_broadcast(&s->cv_done);
     pthread_mutex_unlock(&s->mu);
+}
+
+/* One quantum of the mixed batch over the given idle pooled jobs, on the
+ * pool's stream: the batch is (re)built when the set of jobs changed since
+ * the last build (jobs joined or finished; every job is idle, so no batched
+ * work is in flight), then each job's event is recorded after the quantum. */
+static int pool_quantum(ufoir_server *s, job **jobs, unsigned int n)
+{
+    udev *d = s->ctx->dev;
+    int rc;
+    if (!s->pool_stream && (rc = udev_stream_create(d, &s->pool_stream)))
+        return rc;
+    udev_use_stream(d, s->pool_stream);
+    int same = s->pool && s->n_pool == n;
+    for (unsigned int i = 0; i < n && same; i++)
+        same = s->pool_ids[i] == jobs[i]->id;
+    if (!same) {
+        /* members in id order, so that the same set gives the same batch */
+        for (unsigned int a = 1; a < n; a++) {
+            job *k = jobs[a];
+            unsigned int b = a;
+            while (b > 0 && jobs[b - 1]->id > k->id) {
+                jobs[b] = jobs[b - 1];
+                b--;
+            }
+            jobs[b] = k;
+        }
+        same = s->pool && s->n_pool == n;
+        for (unsigned int i = 0; i < n && same; i++)
+            same = s->pool_ids[i] == jobs[i]->id;
+    }
+    if (!same) {
+        ufoir_batch_destroy(s->pool);
+        s->pool = NULL;
+        s->n_pool = 0;
+        if (n > s->cap_pool) {
+            uint64_t *ids = (uint64_t *) realloc(s->pool_ids, sizeof(uint64_t) * n);
+            if (!ids)
+                return ufoir__fail(s->ctx, UFOIR_ERR_NOMEM, "out of host memory");
+            s->pool_ids = ids;
+            s->cap_pool = n;
+        }
+        ufoir__bmember *m = (ufoir__bmember *) calloc(n, sizeof(*m));
+        if (!m)
+            return ufoir__fail(s->ctx, UFOIR_ERR_NOMEM, "out of host memory");
+        for (unsigned int i = 0; i < n; i++) {
+            job *j = jobs[i];
+            m[i].p = j->proj;
+            m[i].b = j->b;
+            m[i].x = j->x;
+            m[i].R = j->R;
+            m[i].C = j->C;
+            m[i].resid = j->resid;
+            m[i].P = j->sirt.fs.P;
+            m[i].TP = j->sirt.fs.TP;
+            m[i].lambda = j->d.sart.relaxation_factor;
+            m[i].shape_slices = 1;
+            s->pool_ids[i] = j->id;
+        }
+        rc = ufoir__batch_build(s->ctx, m, (int) n, &s->pool);
+        free(m);
+        if (rc)
+            return rc;
+        s->n_pool = n;
+    }
+    /* as many iterations as the quantum, but no member past its count */
+    unsigned int k = s->cfg.quantum ? s->cfg.quantum : 1;
+    for (unsigned int i = 0; i < n; i++) {
+        const unsigned int left = jobs[i]->total_iters - jobs[i]->done_iters;
+        k = left < k ? left : k;
+    }
+    if ((rc = ufoir__batch_launch(s->pool, k)))
+        return rc;
+    s->pool_quanta += k;
+    for (unsigned int i = 0; i < n; i++) {
+        jobs[i]->done_iters += k;
+        if ((rc = udev_event_record(d, jobs[i]->event)))
+            return rc;
+        jobs[i]->busy = 1;
+    }
+    return UFOIR_OK;
 }
 
 /* Removes j (whose predecessor in the queue is prev, NULL at the head) from
@@ -548,8 +653,38 @@ static void *worker_main(void *arg)
             }
             idle[b] = k;
         }
+        /* the idle pooled SIRT jobs advance together: one quantum of the
+         * mixed batch, counted as one job in flight */
+        {
+            job *pool_now[1024];
+            unsigned int n_pool_now = 0, n_rest = 0;
+            for (unsigned int i = 0; i < n_idle; i++) {
+                if (idle[i]->pooled && !s->pool_off)
+                    pool_now[n_pool_now++] = idle[i];
+                else
+                    idle[n_rest++] = idle[i];
+            }
+            n_idle = n_rest;
+            if (n_pool_now > 0 && running < max_running) {
+                const int rc = pool_quantum(s, pool_now, n_pool_now);
+                if (rc != UFOIR_OK) {
+                    /* no batch: these jobs go on with their own graphs */
+                    s->pool_off = 1;
+                    for (unsigned int i = 0; i < n_pool_now; i++)
+                        idle[n_idle++] = pool_now[i];
+                } else {
+                    running++;
+                }
+                progressed = 1;
+            } else {
+                for (unsigned int i = 0; i < n_pool_now; i++)
+                    idle[n_idle++] = pool_now[i];
+            }
+        }
         for (unsigned int i = 0; i < n_idle && running < max_running; i++) {
             job *j = idle[i];
+            if (j->pooled && !s->pool_off)
+                continue;      /* waits for the pool's next quantum */
             const int rc = job_quantum(s, j);
             if (rc != UFOIR_OK) {
                 j->phase = PH_END;
@@ -832,6 +967,7 @@ int ufoir_serve_get_stats(ufoir_server *s, ufoir_serve_stats *o)
     o->rejected = s->rejected;
     o->peak_hbm_bytes = s->peak_reserved;
     o->peak_active_jobs = s->peak_active;
+    o->batched_iterations = s->pool_quanta;
     const size_t n = s->n_lat;
     double *l = n ? (double *) malloc(n * sizeof(double)) : NULL;
     double *q = n ? (double *) malloc(n * sizeof(double)) : NULL;
@@ -878,6 +1014,13 @@ void ufoir_serve_destroy(ufoir_server *s)
     pthread_mutex_unlock(&s->mu);
     if (s->worker_started)
         pthread_join(s->worker, NULL);
+    if (s->pool_stream) {
+        udev_use_stream(s->ctx->dev, s->pool_stream);
+        ufoir_batch_destroy(s->pool);
+        udev_use_stream(s->ctx->dev, NULL);
+        udev_stream_destroy(s->ctx->dev, s->pool_stream);
+    }
+    free(s->pool_ids);
     for (size_t i = 0; i < s->n_jobs; i++)
         free(s->jobs[i]);
     free(s->jobs);

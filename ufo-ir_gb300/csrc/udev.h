@@ -49,6 +49,7 @@ typedef struct {
     const float *d_sin;            /* [n_angles] float LUT */
     const float *d_cos;
     const unsigned char *d_dir;    /* [n_angles] direction of each angle (full subsets) */
+    int fast_arith;                /* 1: the tiled projectors' fast interpolation (not the reference's rounding) */
 } udev_geom;
 
 /* Forward projection of angles [a0, a0 + na) for n_slices slices:
@@ -122,6 +123,55 @@ int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int
 int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, float tile_spread,
                   const float *volP, const float *volTP, const float *src, const float *w, int w_shared,
                   float *out, float scale, int n_slices);
+/* Launch shape of the tiled forward projector. J detector pairs per thread
+ * and angle slot, A angles per tile (the tile list must have been built with
+ * A), win: detector-split CTAs stage column windows, K rows per chunk
+ * (4, 8, 16 or 32), dsplit CTAs per tile; the rest is derived by
+ * udev_fp_cfg_finish. Every shape gives the same results bit for bit: each
+ * ray's arithmetic does not depend on which CTA or lane carries it. */
+typedef struct {
+    int J, A, win, K, dsplit;
+    int threads, dper, wcols, wstride, margin;
+    int fm;                        /* fast arithmetic (from the geometry) */
+    size_t smem;
+} udev_fp_cfg;
+/* The fixed rules (what udev_fp_tiles uses) for n_tiles tiles of the
+ * default angle count and n_slices slices. */
+int udev_fp_default_cfg(udev *d, const udev_geom *g, int n_tiles, int n_slices, float tile_spread, udev_fp_cfg *c);
+/* Fills the derived fields of a shape given J, A, win, K, dsplit;
+ * UFOIR_ERR_UNSUPPORTED if no kernel or not enough shared memory serves it. */
+int udev_fp_cfg_finish(udev *d, const udev_geom *g, float tile_spread, udev_fp_cfg *c);
+/* udev_fp_tiles with an explicit shape. */
+int udev_fp_tiles_cfg(udev *d, const udev_geom *g, const udev_fp_cfg *c, const void *d_tiles, int n_tiles,
+                      const float *volP, const float *volTP, const float *src, const float *w, int w_shared,
+                      float *out, float scale, int n_slices);
+
+/* ---- Mixed batches: one launch per kernel over many one-slice jobs ----
+ * Each job contributes an opaque record (built on the host by *_record,
+ * copied to device memory by the caller) and `items` CTAs; item_start is
+ * the exclusive prefix sum of the items (n_jobs entries, device memory),
+ * job_index maps a record to its entry of the active array (device ints;
+ * 0 = skip the job). */
+size_t udev_fp_record_bytes(void);
+/* 1 if a shape's shared memory leaves room for the batch kernel's record. */
+int udev_fp_batch_fits(const udev *d, const udev_fp_cfg *c);
+int udev_fp_record(udev *d, const udev_geom *g, const udev_fp_cfg *c, const void *d_tiles, int n_tiles,
+                   const float *volP, const float *volTP, const float *src, const float *w, float *out,
+                   float scale, void *record, int *items);
+/* All records must share the launch shape's J, A, win, threads and smem. */
+int udev_fp_batch(udev *d, const udev_fp_cfg *c, const void *d_records, const int *d_item_start, int n_jobs,
+                  const int *d_job_index, const int *d_active, int n_items);
+size_t udev_bp_record_bytes(void);
+int udev_bp_record(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets, const float *sino,
+                   const float *base, const float *cw, const float *add, float *dst, float relax, void *record,
+                   int *items);
+int udev_bp_batch(udev *d, int fast_arith, const void *d_records, const int *d_item_start, int n_jobs,
+                  const int *d_job_index, const int *d_active, int n_items);
+size_t udev_pad_record_bytes(void);
+int udev_pad_record(int n, const float *vol, float *volP, float *volTP, void *record, int *items);
+int udev_pad_batch(udev *d, const void *d_records, const int *d_item_start, int n_jobs, const int *d_job_index,
+                   const int *d_active, int n_items);
+
 /* Backprojection with shared-memory sinogram windows (udev_bp uses it for
  * 16 or more angles); same contract as udev_bp, at most 16 subsets. */
 int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,

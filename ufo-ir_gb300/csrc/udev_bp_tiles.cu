@@ -21,6 +21,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "joseph.cuh"
 #include "udev_internal.cuh"
 
@@ -121,6 +123,7 @@ __device__ __forceinline__ float det_coord(float fX, float fY, float cs, float s
  * that cross the ends of the detector row go element by element, with zeros
  * outside [0, n).
  */
+template <bool FM>
 __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, const float *sino, int x0, int y0,
                            const joseph::AxisConsts &k, float e0, float e1, float shift)
 {
@@ -144,12 +147,14 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
         S.ang[buf][tid] = make_float4(cs, sn, __int_as_float(w0), 0.0f);
     }
     __syncthreads();
-    /* row products of the chunk's angles, rounded as the in-loop product */
+    /* row products of the chunk's angles, rounded as the in-loop product
+     * (fast arithmetic: with the shift already added) */
     float *nys = reinterpret_cast<float *>(&S.nys[buf][0][0][0]);
     for (int idx = tid; idx < count * kTileY; idx += kTX * kTY) {
         const int slot = idx / kTileY, r = idx % kTileY;      /* row r = ty + kTY * p */
         const float nfy = -__fsub_rn(__fadd_rn((float) (y0 + r), 0.5f), k.os);
-        nys[(slot * kTY + r % kTY) * kPY + r / kTY] = __fmul_rn(nfy, S.ang[buf][slot].y);
+        const float prod = __fmul_rn(nfy, S.ang[buf][slot].y);
+        nys[(slot * kTY + r % kTY) * kPY + r / kTY] = FM ? __fadd_rn(prod, shift) : prod;
     }
     constexpr int kGroups = kWin / 4;
     for (int idx = tid; idx < count * kGroups; idx += kTX * kTY) {
@@ -177,7 +182,7 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
  * packed instruction. FAST: every clamped coordinate is >= 0.5, so the
  * three-step floor applies.
  */
-template <bool CLAMP, bool FAST>
+template <bool CLAMP, bool FAST, bool FM>
 __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count, int first_vi, const BpTileArgs &P,
                                              float fX, float shift, float e0, float e1,
                                              float2 sum[kPY / 2], float2 v[kPY / 2], int &sub, int &sub_end)
@@ -211,8 +216,9 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
         const float2 fxc = joseph::splat(__fmul_rn(fX, ang.x));
 #pragma unroll
         for (int q = 0; q < kPY / 2; ++q) {
-            /* fX * cos - fY * sin + shift, as fX*cos + (-fY)*sin + shift */
-            float2 sc = joseph::add2(joseph::add2(fxc, nys[q]), shift2);
+            /* fX * cos - fY * sin + shift, as fX*cos + (-fY)*sin + shift
+             * (fast arithmetic: fX*cos + ((-fY)*sin + shift)) */
+            float2 sc = FM ? joseph::add2(fxc, nys[q]) : joseph::add2(joseph::add2(fxc, nys[q]), shift2);
             if (CLAMP) {
                 sc.x = fminf(fmaxf(sc.x, e0), e1);
                 sc.y = fminf(fmaxf(sc.y, e0), e1);
@@ -223,19 +229,19 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
             const uint32_t a1 = base + 4u * (uint32_t) __float_as_int(y.y);
             const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
             const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
-            sum[q] = joseph::add2(sum[q], joseph::lerp2(t, t0, t1, z2));
+            sum[q] = FM ? joseph::lerp_acc_fast2(sum[q], t, t0, t1) : joseph::add2(sum[q], joseph::lerp2(t, t0, t1, z2));
         }
     }
 }
 
-__global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
+/* One CTA's work: pixel tile `tile` of slice `slice`. */
+template <bool FM>
+__device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile, int slice)
 {
-    __shared__ BpSmem S;
     const int n = P.n;
     const int tiles_x = (n + kTileX - 1) / kTileX;
-    const int x0 = (int) (blockIdx.x % tiles_x) * kTileX;
-    const int y0 = (int) (blockIdx.x / tiles_x) * kTileY;
-    const int slice = (int) blockIdx.y;
+    const int x0 = (tile % tiles_x) * kTileX;
+    const int y0 = (tile / tiles_x) * kTileY;
     const float *sino = P.sino + (size_t) slice * P.sino_stride;
 
     const joseph::AxisConsts k = joseph::axis_consts(n, P.axis);
@@ -278,13 +284,13 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
     int sub = 0;
     int sub_end = P.n_subsets > 0 ? (int) P.sub_n[0] : 0;
     if (nchunks > 0) {
-        load_chunk(P, S, 0, 0, sino, x0, y0, k, e0, e1, shift);
+        load_chunk<FM>(P, S, 0, 0, sino, x0, y0, k, e0, e1, shift);
         cp_async_commit();
     }
     for (int ch = 0; ch < nchunks; ++ch) {
         const int buf = ch & 1;
         if (ch + 1 < nchunks) {
-            load_chunk(P, S, buf ^ 1, ch + 1, sino, x0, y0, k, e0, e1, shift);
+            load_chunk<FM>(P, S, buf ^ 1, ch + 1, sino, x0, y0, k, e0, e1, shift);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -293,11 +299,11 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
         __syncthreads();
         const int count = min(kAC, P.total_angles - ch * kAC);
         if (!clamp)
-            sample_chunk<false, true>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<false, true, FM>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         else if (fast)
-            sample_chunk<true, true>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, true, FM>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         else
-            sample_chunk<true, false>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, false, FM>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         __syncthreads();
     }
     if (P.n_subsets > 0) {
@@ -322,14 +328,62 @@ __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(BpTileArgs P)
     }
 }
 
-}  // namespace
-
-extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
-                             const float *sino, const float *base, const float *cw, int cw_shared, const float *add,
-                             float *dst, float relax, int n_slices)
+template <bool FM>
+__global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(const __grid_constant__ BpTileArgs P)
 {
-    if (n_slices <= 0)
-        return UFOIR_OK;
+    __shared__ BpSmem S;
+    bp_tile<FM>(P, S, (int) blockIdx.x, (int) blockIdx.y);
+}
+
+/*
+ * Mixed batch: the pixel tiles of many one-slice jobs (any size and angle
+ * count) in one launch. CTA b belongs to the job j with item_start[j] <= b <
+ * item_start[j + 1]; its record (the job's BpTileArgs) is staged in shared
+ * memory. Jobs whose active flag is 0 are skipped.
+ */
+template <bool FM>
+__global__ void __launch_bounds__(kTX * kTY, 3) bp_tiles_batch_kernel(const BpTileArgs *__restrict__ recs,
+                                                                   const int *__restrict__ item_start, int n_jobs,
+                                                                   const int *__restrict__ job_index,
+                                                                   const int *__restrict__ active)
+{
+    __shared__ BpSmem S;
+    __shared__ BpTileArgs rec;
+    __shared__ int job_s;
+    const int b = (int) blockIdx.x;
+    const int tid = (int) (threadIdx.y * kTX + threadIdx.x);
+    if (tid == 0) {
+        int lo = 0, hi = n_jobs - 1;      /* last j with item_start[j] <= b */
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(item_start + mid) <= b)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        job_s = lo;
+    }
+    __syncthreads();
+    const int j = job_s;
+    if (!__ldg(active + __ldg(job_index + j)))
+        return;
+    {
+        const int *src = reinterpret_cast<const int *>(recs + j);
+        int *dst = reinterpret_cast<int *>(&rec);
+        for (int e = tid; e < (int) (sizeof(BpTileArgs) / sizeof(int)); e += kTX * kTY)
+            dst[e] = __ldg(src + e);
+    }
+    __syncthreads();
+    bp_tile<FM>(rec, S, b - __ldg(item_start + j), 0);
+}
+
+static_assert(sizeof(BpTileArgs) % sizeof(int) == 0, "records are copied as ints");
+
+/* The arguments of one BP launch (udev_bp_tiles' contract) for one slice. */
+static int fill_args(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets, const float *sino,
+                     const float *base, const float *cw, int cw_shared, const float *add, float *dst, float relax,
+                     BpTileArgs &A)
+{
     if (n_subsets > kMaxSub) {
         udev_set_error(d, "bp_tiles: %d subsets (at most %d)", n_subsets, kMaxSub);
         return UFOIR_ERR_UNSUPPORTED;
@@ -343,8 +397,7 @@ extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *su
         }
         total += (int) subsets[i].n;
     }
-    UDEV_BIND(d);
-    BpTileArgs A;
+    memset(&A, 0, sizeof(A));
     A.sino = sino;
     A.base = base;
     A.cw = cw;
@@ -370,6 +423,57 @@ extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *su
         A.sub_offset[i] = i < n_subsets ? subsets[i].offset : 0;
         A.sub_n[i] = i < n_subsets ? subsets[i].n : 0;
     }
+    return UFOIR_OK;
+}
+
+}  // namespace
+
+extern "C" size_t udev_bp_record_bytes(void)
+{
+    return sizeof(BpTileArgs);
+}
+
+extern "C" int udev_bp_record(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
+                              const float *sino, const float *base, const float *cw, const float *add, float *dst,
+                              float relax, void *record, int *items)
+{
+    BpTileArgs A;
+    const int rc = fill_args(d, g, subsets, n_subsets, sino, base, cw, 0, add, dst, relax, A);
+    if (rc)
+        return rc;
+    memcpy(record, &A, sizeof(A));
+    const int tiles_x = (g->n_dets + kTileX - 1) / kTileX;
+    const int tiles_y = (g->n_dets + kTileY - 1) / kTileY;
+    *items = tiles_x * tiles_y;
+    return UFOIR_OK;
+}
+
+extern "C" int udev_bp_batch(udev *d, int fast_arith, const void *d_records, const int *d_item_start, int n_jobs,
+                             const int *d_job_index, const int *d_active, int n_items)
+{
+    if (n_jobs <= 0 || n_items <= 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    if (fast_arith)
+        bp_tiles_batch_kernel<true><<<(unsigned int) n_items, dim3(kTX, kTY), 0, d->stream>>>(
+            static_cast<const BpTileArgs *>(d_records), d_item_start, n_jobs, d_job_index, d_active);
+    else
+        bp_tiles_batch_kernel<false><<<(unsigned int) n_items, dim3(kTX, kTY), 0, d->stream>>>(
+            static_cast<const BpTileArgs *>(d_records), d_item_start, n_jobs, d_job_index, d_active);
+    return udev_after_launch(d, "bp_tiles_batch_kernel");
+}
+
+extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *subsets, int n_subsets,
+                             const float *sino, const float *base, const float *cw, int cw_shared, const float *add,
+                             float *dst, float relax, int n_slices)
+{
+    if (n_slices <= 0)
+        return UFOIR_OK;
+    BpTileArgs A;
+    const int rc0 = fill_args(d, g, subsets, n_subsets, sino, base, cw, cw_shared, add, dst, relax, A);
+    if (rc0)
+        return rc0;
+    UDEV_BIND(d);
     const int tiles_x = (g->n_dets + kTileX - 1) / kTileX;
     const int tiles_y = (g->n_dets + kTileY - 1) / kTileY;
     const unsigned int n_tiles = (unsigned int) (tiles_x * tiles_y);
@@ -384,7 +488,10 @@ extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *su
         if (B.add)
             B.add += (size_t) done * A.vol_stride;
         B.dst += (size_t) done * A.vol_stride;
-        bp_tiles_kernel<<<dim3(n_tiles, (unsigned int) chunk), dim3(kTX, kTY), 0, d->stream>>>(B);
+        if (g->fast_arith)
+            bp_tiles_kernel<true><<<dim3(n_tiles, (unsigned int) chunk), dim3(kTX, kTY), 0, d->stream>>>(B);
+        else
+            bp_tiles_kernel<false><<<dim3(n_tiles, (unsigned int) chunk), dim3(kTX, kTY), 0, d->stream>>>(B);
         int rc = udev_after_launch(d, "bp_tiles_kernel");
         if (rc)
             return rc;

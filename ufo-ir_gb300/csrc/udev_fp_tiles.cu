@@ -30,6 +30,9 @@
  */
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <cstring>
+
 #include "joseph.cuh"
 #include "tma.cuh"
 #include "udev_internal.cuh"
@@ -68,16 +71,21 @@ struct FpTileArgs {
     int *err;
 };
 
+static_assert(sizeof(FpTileArgs) % sizeof(int) == 0, "records are copied as ints");
+/* static shared memory of the batch kernel (its record and job index), rounded up */
+constexpr size_t kBatchStatic = (sizeof(FpTileArgs) + 16 + 127) / 128 * 128;
+
 constexpr int kMaxWinThreads = 448;   /* detector-split CTAs hold at most half the slots */
 
 /* Windowed CTAs of the J = 1 variants made for large n (A <= 4) hold few
  * rays per thread: two of them per SM. (The A = 8 variant, the default at
  * n <= 768, measured 4 % slower held to that register budget.) */
-template <int J, int A, bool WIN>
-__global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && A <= 4) ? 2 : 1)
-    fp_tiles_kernel(FpTileArgs P)
+/* One CTA's work: angle tile `tile_idx` of P.tiles, detector part `dpart`
+ * of P.dsplit, slice `slice`; smem_raw is the dynamic shared memory. */
+template <int J, int A, bool WIN, bool FM>
+__device__ __forceinline__ void fp_tile(const FpTileArgs &P, int tile_idx, int dpart, int slice,
+                                        unsigned char *smem_raw)
 {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
     int *w0s = reinterpret_cast<int *>(smem_raw + 16);     /* window start of each stage */
     float *ext = reinterpret_cast<float *>(smem_raw + 32);   /* [3][A]: extreme rays' starts, steps */
@@ -89,12 +97,11 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
     constexpr bool win = WIN;
     const size_t stage_floats = (size_t) K * wstride;
 
-    const int4 tile = P.tiles[blockIdx.x / (unsigned) P.dsplit];
-    const int slice = (int) blockIdx.y;
+    const int4 tile = P.tiles[tile_idx];
     const int n = P.n;
     const int dir = tile.z;
     /* detector range of this CTA: [dstart, dend) */
-    const int dstart = (int) (blockIdx.x % (unsigned) P.dsplit) * P.dper;
+    const int dstart = dpart * P.dper;
     const int dend = min(n, dstart + P.dper);
     const float *img = (dir == 0 ? P.volTP : P.volP) + (size_t) slice * P.volp_stride;
 
@@ -271,7 +278,8 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
                             const uint32_t a1 = base + 4u * (uint32_t) __float_as_int(y.y);
                             const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
                             const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
-                            inner[k][m] = joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
+                            inner[k][m] = FM ? joseph::lerp_acc_fast2(inner[k][m], t, t0, t1)
+                                             : joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
                             c[k][m] = joseph::add2(c[k][m], stp[k]);
                         }
                     }
@@ -298,7 +306,8 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
                             const uint32_t a0 = row_s + 4u * p0, a1 = row_s + 4u * p1;
                             const float2 t0 = make_float2(joseph::lds(a0), joseph::lds(a1));
                             const float2 t1 = make_float2(joseph::lds(a0 + 4u), joseph::lds(a1 + 4u));
-                            inner[k][m] = joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
+                            inner[k][m] = FM ? joseph::lerp_acc_fast2(inner[k][m], t, t0, t1)
+                                             : joseph::add2(inner[k][m], joseph::lerp2(t, t0, t1, z2));
                             c[k][m] = joseph::add2(c[k][m], stp[k]);
                         }
                     }
@@ -363,6 +372,56 @@ __global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && 
     }
 }
 
+template <int J, int A, bool WIN, bool FM>
+__global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && A <= 4) ? 2 : 1)
+    fp_tiles_kernel(const __grid_constant__ FpTileArgs P)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    fp_tile<J, A, WIN, FM>(P, (int) (blockIdx.x / (unsigned) P.dsplit), (int) (blockIdx.x % (unsigned) P.dsplit),
+                       (int) blockIdx.y, smem_raw);
+}
+
+/*
+ * Mixed batch: the tiles of many one-slice jobs (any n_angles, same launch
+ * shape) in one launch. CTA b belongs to the job j with item_start[j] <= b <
+ * item_start[j + 1]; its record (the job's FpTileArgs) is staged in shared
+ * memory. Jobs whose active flag is 0 are skipped.
+ */
+template <int J, int A, bool WIN, bool FM>
+__global__ void __launch_bounds__(WIN ? kMaxWinThreads : 768, (WIN && J == 1 && A <= 4) ? 2 : 1)
+    fp_tiles_batch_kernel(const FpTileArgs *__restrict__ recs, const int *__restrict__ item_start, int n_jobs,
+                          const int *__restrict__ job_index, const int *__restrict__ active)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ FpTileArgs rec;
+    __shared__ int job_s;
+    const int b = (int) blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n_jobs - 1;      /* last j with item_start[j] <= b */
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(item_start + mid) <= b)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        job_s = lo;
+    }
+    __syncthreads();
+    const int j = job_s;
+    if (!__ldg(active + __ldg(job_index + j)))
+        return;
+    {
+        const int *src = reinterpret_cast<const int *>(recs + j);
+        int *dst = reinterpret_cast<int *>(&rec);
+        for (int e = (int) threadIdx.x; e < (int) (sizeof(FpTileArgs) / sizeof(int)); e += (int) blockDim.x)
+            dst[e] = __ldg(src + e);
+    }
+    __syncthreads();
+    const int local = b - __ldg(item_start + j);
+    fp_tile<J, A, WIN, FM>(rec, local / rec.dsplit, local % rec.dsplit, 0, smem_raw);
+}
+
 /* Writes the padded copy and the padded transpose of n x n slices; the pad
  * columns are left as they are (zeroed once when the buffers are made). */
 __global__ void __launch_bounds__(256) pad_transpose_kernel(const float *__restrict__ in, float *__restrict__ outP,
@@ -413,7 +472,7 @@ TileCfg tile_cfg(int n, int smem_optin)
     return c;
 }
 
-template <int J, int A, bool WIN>
+template <int J, int A, bool WIN, bool FM>
 int launch_tiles(udev *d, const FpTileArgs &args, int n_tiles, int n_slices, int threads, size_t smem)
 {
     for (int done = 0; done < n_slices;) {
@@ -426,7 +485,7 @@ int launch_tiles(udev *d, const FpTileArgs &args, int n_tiles, int n_slices, int
         if (B.w)
             B.w += (size_t) done * args.w_stride;
         const dim3 grid((unsigned int) (n_tiles * args.dsplit), (unsigned int) chunk);
-        fp_tiles_kernel<J, A, WIN><<<grid, threads, smem, d->stream>>>(B);
+        fp_tiles_kernel<J, A, WIN, FM><<<grid, threads, smem, d->stream>>>(B);
         int rc = udev_after_launch(d, "fp_tiles_kernel");
         if (rc)
             return rc;
@@ -453,29 +512,41 @@ extern "C" int udev_fp_tile_angles(udev *d, int n)
     return tiles_supported(cfg, d->smem_optin) ? cfg.A : 0;
 }
 
+template <bool FM>
+static int kernels_init_fm(udev *d)
+{
+#define UDEV_TILE_ATTR(K_, bytes)                                                                              \
+    UDEV_CHECK(d, cudaFuncSetAttribute(K_, cudaFuncAttributeMaxDynamicSharedMemorySize, (bytes)))
+    UDEV_TILE_ATTR((fp_tiles_kernel<1, 8, false, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<2, 8, false, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<4, 4, false, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<8, 2, false, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<1, 8, true, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<2, 8, true, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<4, 4, true, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<8, 2, true, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<1, 4, true, FM>), d->smem_optin);
+    UDEV_TILE_ATTR((fp_tiles_kernel<1, 2, true, FM>), d->smem_optin);
+    /* the batch kernels also hold their record in static shared memory */
+    const int batch_dyn = d->smem_optin - (int) kBatchStatic;
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<1, 8, false, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<2, 8, false, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<4, 4, false, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<8, 2, false, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<1, 8, true, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<2, 8, true, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<4, 4, true, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<8, 2, true, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<1, 4, true, FM>), batch_dyn);
+    UDEV_TILE_ATTR((fp_tiles_batch_kernel<1, 2, true, FM>), batch_dyn);
+#undef UDEV_TILE_ATTR
+    return UFOIR_OK;
+}
+
 int udev_kernels_init(udev *d)
 {
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<2, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<4, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<8, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<2, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<4, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<8, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    UDEV_CHECK(d, cudaFuncSetAttribute(fp_tiles_kernel<1, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       d->smem_optin));
-    return UFOIR_OK;
+    int rc = kernels_init_fm<false>(d);
+    return rc ? rc : kernels_init_fm<true>(d);
 }
 
 extern "C" int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int n, int n_slices)
@@ -498,19 +569,130 @@ extern "C" int udev_pad_transpose(udev *d, const float *vol, float *volP, float 
     return UFOIR_OK;
 }
 
-extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, float tile_spread,
-                             const float *volP, const float *volTP, const float *src, const float *w, int w_shared,
-                             float *out, float scale, int n_slices)
+/* The template variants that exist: (J, A) with whole rows, and the
+ * windowed ones of split tiles. */
+static bool variant_exists(int J, int A, bool win)
 {
-    if (n_slices <= 0 || n_tiles <= 0)
-        return UFOIR_OK;
-    UDEV_BIND(d);
+    const int k = J * 16 + A;
+    if (!win)
+        return k == 1 * 16 + 8 || k == 2 * 16 + 8 || k == 4 * 16 + 4 || k == 8 * 16 + 2;
+    return k == 1 * 16 + 2 || k == 1 * 16 + 4 || k == 1 * 16 + 8 || k == 2 * 16 + 8 || k == 4 * 16 + 4 ||
+           k == 8 * 16 + 2;
+}
+
+extern "C" int udev_fp_cfg_finish(udev *d, const udev_geom *g, float tile_spread, udev_fp_cfg *c)
+{
+    const int n = g->n_dets, pitch = udev_fp_pitch(n);
+    c->fm = g->fast_arith ? 1 : 0;
+    if (!variant_exists(c->J, c->A, c->win != 0) || (c->K != 4 && c->K != 8 && c->K != 16 && c->K != 32) ||
+        c->dsplit < 1 || c->dsplit > 64 || (c->win && c->dsplit < 2))
+        return UFOIR_ERR_UNSUPPORTED;
+    c->dper = (n + c->dsplit - 1) / c->dsplit;
+    const int slots = (c->dper + 2 * c->J - 1) / (2 * c->J);
+    c->threads = (slots + 15) / 16 * 32;
+    if (c->threads > (c->win ? kMaxWinThreads : kMaxTileThreads))
+        return UFOIR_ERR_UNSUPPORTED;
+    c->margin = 4 + n / 512;
+    c->wcols = c->wstride = pitch;
+    if (c->win) {
+        /* the columns a chunk's rays can reach: the detector range times
+         * max |det_step| = sqrt 2, the chunk's rows times max |step| = 1,
+         * the spread of the tile's angles, and a margin */
+        const double need = (double) (c->dper - 1) * 1.41422 + (double) (c->K - 1) + (double) tile_spread +
+                            2.0 * c->margin + 8.0;
+        const int wc = ((int) ceil(need) + 3) / 4 * 4;
+        if (wc >= pitch)
+            return UFOIR_ERR_UNSUPPORTED;
+        c->wcols = wc;
+        c->wstride = wc + 4;
+    }
+    c->smem = kHeader + 2 * (size_t) c->K * c->wstride * 4;
+    if (c->smem > (size_t) d->smem_optin)
+        return UFOIR_ERR_UNSUPPORTED;
+    return UFOIR_OK;
+}
+
+extern "C" int udev_fp_default_cfg(udev *d, const udev_geom *g, int n_tiles, int n_slices, float tile_spread,
+                                   udev_fp_cfg *c)
+{
     const int n = g->n_dets;
     const TileCfg cfg = tile_cfg(n, d->smem_optin);
     if (!tiles_supported(cfg, d->smem_optin)) {
         udev_set_error(d, "fp_tiles: n_dets %d needs %d threads / %zu B shared memory", n, cfg.threads, cfg.smem);
         return UFOIR_ERR_UNSUPPORTED;
     }
+    const int pitch = udev_fp_pitch(n);
+    c->fm = g->fast_arith ? 1 : 0;
+    c->J = cfg.J;
+    c->A = cfg.A;
+    c->win = 0;
+    c->K = cfg.K;
+    c->dsplit = 1;
+    c->dper = n;
+    c->threads = cfg.threads;
+    c->wcols = c->wstride = pitch;
+    c->margin = 4 + n / 512;
+    c->smem = cfg.smem;
+    /* Too few tiles to fill the GPU (one slice, few angles): split each
+     * angle tile's detectors over up to 8 CTAs, with chunks small enough
+     * for two CTAs per SM. Every CTA walks all rows; it stages only the
+     * window of columns its rays can reach (the detector range times
+     * max |det_step| = sqrt 2, the chunk's rows times max |step| = 1, the
+     * spread of the tile's angles, and a margin), unless that is the whole
+     * row. */
+    const long long ctas = (long long) n_tiles * n_slices;
+    if (ctas < d->sm_count) {
+        int split = (int) ((2LL * d->sm_count + ctas - 1) / ctas);
+        split = split > 8 ? 8 : split;
+        while (split > 1 && (n + split - 1) / split < 64)
+            split--;
+        int k2 = cfg.K;
+        while (k2 > 4 && 2 * (kHeader + 2 * (size_t) k2 * pitch * 4) > (size_t) d->smem_optin)
+            k2 /= 2;
+        if (split > 1 && 2 * (kHeader + 2 * (size_t) k2 * pitch * 4) <= (size_t) d->smem_optin) {
+            c->dsplit = split;
+            c->dper = (n + split - 1) / split;
+            const int slots = (c->dper + 2 * cfg.J - 1) / (2 * cfg.J);
+            c->threads = (slots + 15) / 16 * 32;
+            c->K = k2;
+            c->smem = kHeader + 2 * (size_t) k2 * pitch * 4;
+            /* Windowed CTAs take one detector pair per angle slot (J = 1)
+             * where that fits: a split CTA holds few rays, and at J = 4
+             * (n = 2900) it would run 3 warps of 16 rays per thread, too few
+             * warps to hide the loads. The window: the largest chunk that
+             * keeps two CTAs per SM. */
+            const int slots1 = (c->dper + 1) / 2, threads1 = (slots1 + 15) / 16 * 32;
+            for (int kw = 32; kw >= 4; kw /= 2) {
+                udev_fp_cfg w = *c;
+                w.win = 1;
+                w.K = kw;
+                w.J = threads1 <= kMaxWinThreads ? 1 : cfg.J;
+                if (udev_fp_cfg_finish(d, g, tile_spread, &w) != UFOIR_OK) {
+                    if (w.wcols >= pitch)
+                        break;
+                    continue;
+                }
+                if (2 * w.smem <= (size_t) d->smem_optin) {
+                    *c = w;
+                    break;
+                }
+            }
+        }
+    }
+    return UFOIR_OK;
+}
+
+template <bool FM>
+static int dispatch_tiles(udev *d, const FpTileArgs &A, const udev_fp_cfg *c, int n_tiles, int n_slices);
+
+extern "C" int udev_fp_tiles_cfg(udev *d, const udev_geom *g, const udev_fp_cfg *c, const void *d_tiles,
+                                 int n_tiles, const float *volP, const float *volTP, const float *src,
+                                 const float *w, int w_shared, float *out, float scale, int n_slices)
+{
+    if (n_slices <= 0 || n_tiles <= 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    const int n = g->n_dets;
     FpTileArgs A;
     A.volP = volP;
     A.volTP = volTP;
@@ -522,7 +704,7 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
     A.tiles = static_cast<const int4 *>(d_tiles);
     A.n = n;
     A.pitch = udev_fp_pitch(n);
-    A.rows_per_chunk = cfg.K;
+    A.rows_per_chunk = c->K;
     A.axis = g->axis;
     A.scale = scale;
     A.volp_stride = (long long) n * A.pitch;
@@ -532,80 +714,229 @@ extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, i
     A.err = d->d_err;
     A.skip_chunk = d->inject_skip_chunk;   /* one-shot test injection */
     d->inject_skip_chunk = -1;
-    /* Too few tiles to fill the GPU (one slice, few angles): split each
-     * angle tile's detectors over up to 8 CTAs, with chunks small enough
-     * for two CTAs per SM. Every CTA walks all rows; it stages only the
-     * window of columns its rays can reach (the detector range times
-     * max |det_step| = sqrt 2, the chunk's rows times max |step| = 1, the
-     * spread of the tile's angles, and a margin), unless that is the whole
-     * row. */
-    int threads = cfg.threads, K = cfg.K, win_j = cfg.J;
-    A.dsplit = 1;
-    A.dper = n;
-    A.wcols = A.pitch;
-    A.wstride = A.pitch;
-    A.margin = 4 + n / 512;
-    const long long ctas = (long long) n_tiles * n_slices;
-    if (ctas < d->sm_count) {
-        int split = (int) ((2LL * d->sm_count + ctas - 1) / ctas);
-        split = split > 8 ? 8 : split;
-        while (split > 1 && (n + split - 1) / split < 64)
-            split--;
-        int k2 = K;
-        while (k2 > 4 && 2 * (kHeader + 2 * (size_t) k2 * A.pitch * 4) > (size_t) d->smem_optin)
-            k2 /= 2;
-        if (split > 1 && 2 * (kHeader + 2 * (size_t) k2 * A.pitch * 4) <= (size_t) d->smem_optin) {
-            A.dsplit = split;
-            A.dper = (n + split - 1) / split;
-            const int slots = (A.dper + 2 * cfg.J - 1) / (2 * cfg.J);
-            threads = (slots + 15) / 16 * 32;
-            K = k2;
-            /* Windowed CTAs take one detector pair per angle slot (J = 1)
-             * where that fits: a split CTA holds few rays, and at J = 4
-             * (n = 2900) it would run 3 warps of 16 rays per thread, too few
-             * warps to hide the loads. */
-            const int slots1 = (A.dper + 1) / 2, threads1 = (slots1 + 15) / 16 * 32;
-            const int threads_win = threads1 <= kMaxWinThreads ? threads1 : threads;
-            /* the column window, with the largest chunk that keeps two CTAs per SM */
-            for (int kw = 32; kw >= 4; kw /= 2) {
-                const double need = (double) (A.dper - 1) * 1.41422 + (double) (kw - 1) + (double) tile_spread +
-                                    2.0 * A.margin + 8.0;
-                const int wc = ((int) ceil(need) + 3) / 4 * 4;
-                if (wc >= A.pitch)
-                    break;
-                if (threads_win <= kMaxWinThreads &&
-                    2 * (kHeader + 2 * (size_t) kw * (wc + 4) * 4) <= (size_t) d->smem_optin) {
-                    A.wcols = wc;
-                    A.wstride = wc + 4;
-                    K = kw;
-                    if (threads_win == threads1)
-                        win_j = 1;
-                    threads = threads_win;
-                    break;
-                }
-            }
+    A.dsplit = c->dsplit;
+    A.dper = c->dper;
+    A.wcols = c->wcols;
+    A.wstride = c->wstride;
+    A.margin = c->margin;
+    return c->fm ? dispatch_tiles<true>(d, A, c, n_tiles, n_slices) : dispatch_tiles<false>(d, A, c, n_tiles, n_slices);
+}
+
+template <bool FM>
+static int dispatch_tiles(udev *d, const FpTileArgs &A, const udev_fp_cfg *c, int n_tiles, int n_slices)
+{
+    if (c->win) {
+        switch (c->J * 16 + c->A) {
+        case 1 * 16 + 4: return launch_tiles<1, 4, true, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 1 * 16 + 2: return launch_tiles<1, 2, true, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 1 * 16 + 8: return launch_tiles<1, 8, true, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 2 * 16 + 8: return launch_tiles<2, 8, true, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 4 * 16 + 4: return launch_tiles<4, 4, true, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 8 * 16 + 2: return launch_tiles<8, 2, true, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        default: break;
         }
-    }
-    A.rows_per_chunk = K;
-    const size_t smem = kHeader + 2 * (size_t) K * A.wstride * 4;
-    if (A.wcols < A.pitch) {
-        switch (win_j * 16 + cfg.A) {
-        case 1 * 16 + 4: return launch_tiles<1, 4, true>(d, A, n_tiles, n_slices, threads, smem);
-        case 1 * 16 + 2: return launch_tiles<1, 2, true>(d, A, n_tiles, n_slices, threads, smem);
-        case 1 * 16 + 8: return launch_tiles<1, 8, true>(d, A, n_tiles, n_slices, threads, smem);
-        case 2 * 16 + 8: return launch_tiles<2, 8, true>(d, A, n_tiles, n_slices, threads, smem);
-        case 4 * 16 + 4: return launch_tiles<4, 4, true>(d, A, n_tiles, n_slices, threads, smem);
-        case 8 * 16 + 2: return launch_tiles<8, 2, true>(d, A, n_tiles, n_slices, threads, smem);
+    } else {
+        switch (c->J * 16 + c->A) {
+        case 1 * 16 + 8: return launch_tiles<1, 8, false, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 2 * 16 + 8: return launch_tiles<2, 8, false, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 4 * 16 + 4: return launch_tiles<4, 4, false, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
+        case 8 * 16 + 2: return launch_tiles<8, 2, false, FM>(d, A, n_tiles, n_slices, c->threads, c->smem);
         default: break;
         }
     }
-    switch (cfg.J * 16 + cfg.A) {
-    case 1 * 16 + 8: return launch_tiles<1, 8, false>(d, A, n_tiles, n_slices, threads, smem);
-    case 2 * 16 + 8: return launch_tiles<2, 8, false>(d, A, n_tiles, n_slices, threads, smem);
-    case 4 * 16 + 4: return launch_tiles<4, 4, false>(d, A, n_tiles, n_slices, threads, smem);
-    case 8 * 16 + 2: return launch_tiles<8, 2, false>(d, A, n_tiles, n_slices, threads, smem);
-    default:
-        udev_set_error(d, "fp_tiles: no kernel for J=%d A=%d", cfg.J, cfg.A);
+    udev_set_error(d, "fp_tiles: no kernel for J=%d A=%d win=%d", c->J, c->A, c->win);
+    return UFOIR_ERR_UNSUPPORTED;
+}
+
+extern "C" int udev_fp_tiles(udev *d, const udev_geom *g, const void *d_tiles, int n_tiles, float tile_spread,
+                             const float *volP, const float *volTP, const float *src, const float *w, int w_shared,
+                             float *out, float scale, int n_slices)
+{
+    if (n_slices <= 0 || n_tiles <= 0)
+        return UFOIR_OK;
+    udev_fp_cfg c;
+    const int rc = udev_fp_default_cfg(d, g, n_tiles, n_slices, tile_spread, &c);
+    if (rc)
+        return rc;
+    return udev_fp_tiles_cfg(d, g, &c, d_tiles, n_tiles, volP, volTP, src, w, w_shared, out, scale, n_slices);
+}
+
+/* ---- mixed batches ---- */
+
+extern "C" size_t udev_fp_record_bytes(void)
+{
+    return sizeof(FpTileArgs);
+}
+
+extern "C" int udev_fp_batch_fits(const udev *d, const udev_fp_cfg *c)
+{
+    return c->smem + kBatchStatic <= (size_t) d->smem_optin;
+}
+
+extern "C" int udev_fp_record(udev *d, const udev_geom *g, const udev_fp_cfg *c, const void *d_tiles, int n_tiles,
+                              const float *volP, const float *volTP, const float *src, const float *w,
+                              float *out, float scale, void *record, int *items)
+{
+    if (n_tiles <= 0 || !variant_exists(c->J, c->A, c->win != 0) || !udev_fp_batch_fits(d, c))
+        return UFOIR_ERR_UNSUPPORTED;
+    FpTileArgs A;
+    memset(&A, 0, sizeof(A));
+    const int n = g->n_dets;
+    A.volP = volP;
+    A.volTP = volTP;
+    A.src = src;
+    A.w = w;
+    A.out = out;
+    A.sinv = g->d_sin;
+    A.cosv = g->d_cos;
+    A.tiles = static_cast<const int4 *>(d_tiles);
+    A.n = n;
+    A.pitch = udev_fp_pitch(n);
+    A.rows_per_chunk = c->K;
+    A.axis = g->axis;
+    A.scale = scale;
+    A.volp_stride = (long long) n * A.pitch;
+    A.sino_stride = (long long) g->n_angles * n;
+    A.w_stride = 0;
+    A.neg_zero = -0.0f;
+    A.err = d->d_err;
+    A.skip_chunk = -1;
+    A.dsplit = c->dsplit;
+    A.dper = c->dper;
+    A.wcols = c->wcols;
+    A.wstride = c->wstride;
+    A.margin = c->margin;
+    memcpy(record, &A, sizeof(A));
+    *items = n_tiles * c->dsplit;
+    return UFOIR_OK;
+}
+
+template <int J, int A, bool WIN, bool FM>
+static int launch_batch(udev *d, const udev_fp_cfg *c, const void *recs, const int *item_start, int n_jobs,
+                        const int *job_index, const int *active, int n_items)
+{
+    fp_tiles_batch_kernel<J, A, WIN, FM><<<(unsigned int) n_items, c->threads, c->smem, d->stream>>>(
+        static_cast<const FpTileArgs *>(recs), item_start, n_jobs, job_index, active);
+    return udev_after_launch(d, "fp_tiles_batch_kernel");
+}
+
+template <bool FM>
+static int dispatch_batch(udev *d, const udev_fp_cfg *c, const void *r, const int *st, int nj, const int *ji,
+                          const int *ac, int ni)
+{
+    if (c->win) {
+        switch (c->J * 16 + c->A) {
+        case 1 * 16 + 4: return launch_batch<1, 4, true, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 1 * 16 + 2: return launch_batch<1, 2, true, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 1 * 16 + 8: return launch_batch<1, 8, true, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 2 * 16 + 8: return launch_batch<2, 8, true, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 4 * 16 + 4: return launch_batch<4, 4, true, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 8 * 16 + 2: return launch_batch<8, 2, true, FM>(d, c, r, st, nj, ji, ac, ni);
+        default: break;
+        }
+    } else {
+        switch (c->J * 16 + c->A) {
+        case 1 * 16 + 8: return launch_batch<1, 8, false, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 2 * 16 + 8: return launch_batch<2, 8, false, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 4 * 16 + 4: return launch_batch<4, 4, false, FM>(d, c, r, st, nj, ji, ac, ni);
+        case 8 * 16 + 2: return launch_batch<8, 2, false, FM>(d, c, r, st, nj, ji, ac, ni);
+        default: break;
+        }
+    }
+    udev_set_error(d, "fp_tiles batch: no kernel for J=%d A=%d win=%d", c->J, c->A, c->win);
+    return UFOIR_ERR_UNSUPPORTED;
+}
+
+extern "C" int udev_fp_batch(udev *d, const udev_fp_cfg *c, const void *d_records, const int *d_item_start,
+                             int n_jobs, const int *d_job_index, const int *d_active, int n_items)
+{
+    if (n_jobs <= 0 || n_items <= 0)
+        return UFOIR_OK;
+    if (!udev_fp_batch_fits(d, c)) {
+        udev_set_error(d, "fp_tiles batch: %zu B of shared memory do not fit", c->smem);
         return UFOIR_ERR_UNSUPPORTED;
     }
+    UDEV_BIND(d);
+    return c->fm ? dispatch_batch<true>(d, c, d_records, d_item_start, n_jobs, d_job_index, d_active, n_items)
+                 : dispatch_batch<false>(d, c, d_records, d_item_start, n_jobs, d_job_index, d_active, n_items);
+}
+
+/* Padded copies of the volumes of a mixed batch: one launch, 32 x 32 tiles. */
+struct PadRec {
+    const float *vol;
+    float *P, *TP;
+    int n, pitch, tiles_x, pad_;
+};
+
+__global__ void __launch_bounds__(256) pad_batch_kernel(const PadRec *__restrict__ recs,
+                                                        const int *__restrict__ item_start, int n_jobs,
+                                                        const int *__restrict__ job_index,
+                                                        const int *__restrict__ active)
+{
+    __shared__ float tile[32][33];
+    __shared__ int job_s;
+    const int b = (int) blockIdx.x;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        int lo = 0, hi = n_jobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(item_start + mid) <= b)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        job_s = lo;
+    }
+    __syncthreads();
+    const int j = job_s;
+    if (!__ldg(active + __ldg(job_index + j)))
+        return;
+    const PadRec r = recs[j];
+    const int local = b - __ldg(item_start + j);
+    const int bx = (local % r.tiles_x) * 32, by = (local / r.tiles_x) * 32;
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int x = bx + threadIdx.x, y = by + k;
+        if (x < r.n && y < r.n) {
+            const float v = r.vol[(size_t) y * r.n + x];
+            tile[k][threadIdx.x] = v;
+            r.P[(size_t) y * r.pitch + kPadL + x] = v;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int x = by + threadIdx.x, y = bx + k;
+        if (x < r.n && y < r.n)
+            r.TP[(size_t) y * r.pitch + kPadL + x] = tile[threadIdx.x][k];
+    }
+}
+
+extern "C" size_t udev_pad_record_bytes(void)
+{
+    return sizeof(PadRec);
+}
+
+extern "C" int udev_pad_record(int n, const float *vol, float *volP, float *volTP, void *record, int *items)
+{
+    PadRec r;
+    memset(&r, 0, sizeof(r));
+    r.vol = vol;
+    r.P = volP;
+    r.TP = volTP;
+    r.n = n;
+    r.pitch = udev_fp_pitch(n);
+    r.tiles_x = (n + 31) / 32;
+    memcpy(record, &r, sizeof(r));
+    *items = r.tiles_x * r.tiles_x;
+    return UFOIR_OK;
+}
+
+extern "C" int udev_pad_batch(udev *d, const void *d_records, const int *d_item_start, int n_jobs,
+                              const int *d_job_index, const int *d_active, int n_items)
+{
+    if (n_jobs <= 0 || n_items <= 0)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    pad_batch_kernel<<<(unsigned int) n_items, dim3(32, 8), 0, d->stream>>>(
+        static_cast<const PadRec *>(d_records), d_item_start, n_jobs, d_job_index, d_active);
+    return udev_after_launch(d, "pad_batch_kernel");
 }

@@ -36,6 +36,8 @@ HORIZONTAL = 0
 VERTICAL = 1
 NORM_COMPAT = 0
 NORM_FP64 = 1
+ARITH_EXACT = 0
+ARITH_FAST = 1
 
 
 class UfoirError(RuntimeError):
@@ -47,7 +49,7 @@ class UfoirError(RuntimeError):
 class ProjectorParams(C.Structure):
     _fields_ = [("model", C.c_char * 32), ("angles_num", C.c_uint), ("is_forward", C.c_int),
                 ("axis_position", C.c_float), ("step", C.c_float), ("relaxation", C.c_float),
-                ("correction_scale", C.c_float)]
+                ("correction_scale", C.c_float), ("arithmetic", C.c_int)]
 
 
 class Subset(C.Structure):
@@ -70,6 +72,21 @@ class AsdpocsParams(C.Structure):
 
 class AsdpocsScalars(C.Structure):
     _fields_ = [("dp", C.c_float), ("dd", C.c_float), ("dg", C.c_float), ("dtgv", C.c_float)]
+
+
+class FpTuning(C.Structure):
+    _fields_ = [("J", C.c_int), ("A", C.c_int), ("win", C.c_int), ("K", C.c_int), ("dsplit", C.c_int),
+                ("threads", C.c_int), ("tuned", C.c_int), ("candidates", C.c_uint), ("ms_default", C.c_float),
+                ("ms_tuned", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchJob(C.Structure):
+    _fields_ = [("n_dets", C.c_uint), ("n_angles", C.c_uint), ("step", C.c_float), ("axis_position", C.c_float),
+                ("relaxation_factor", C.c_float), ("sino", C.c_void_p), ("vol", C.c_void_p), ("keep_vol", C.c_int),
+                ("arithmetic", C.c_int)]
 
 
 class SbtvParams(C.Structure):
@@ -104,7 +121,7 @@ class JobDesc(C.Structure):
 class ServeConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_uint), ("policy", C.c_int),
                 ("quantum", C.c_uint), ("fail_allocation_every", C.c_uint), ("max_running", C.c_uint),
-                ("admit_age_ms", C.c_uint)]
+                ("admit_age_ms", C.c_uint), ("batch_sirt", C.c_uint)]
 
 
 class ServeStats(C.Structure):
@@ -113,7 +130,8 @@ class ServeStats(C.Structure):
                 ("p99_latency_ms", C.c_double), ("mean_latency_ms", C.c_double), ("max_latency_ms", C.c_double),
                 ("p50_queue_ms", C.c_double), ("p99_queue_ms", C.c_double),
                 ("throughput_jobs_per_s", C.c_double), ("busy_seconds", C.c_double),
-                ("peak_hbm_bytes", C.c_uint64), ("peak_active_jobs", C.c_uint)]
+                ("peak_hbm_bytes", C.c_uint64), ("peak_active_jobs", C.c_uint),
+                ("batched_iterations", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -142,6 +160,8 @@ EXPORTED = (
     "ufoir_graph_job_desc", "ufoir_graph_run", "ufoir_io_last_error", "ufoir_io_tiff_info", "ufoir_io_read_tiff",
     "ufoir_io_write_tiff", "ufoir_io_read_raw", "ufoir_io_write_raw", "ufoir_sample_ceiling", "ufoir_sample_ceiling_bp",
     "ufoir_asdpocs_process_ex", "ufoir_tv_gradient", "ufoir_ctx_inject_copy_timeout",
+    "ufoir_ctx_set_autotune", "ufoir_projector_autotune", "ufoir_batch_create", "ufoir_batch_run",
+    "ufoir_batch_set_active", "ufoir_batch_launches", "ufoir_batch_destroy", "ufoir_ctx_sm_count",
 )
 
 
@@ -239,6 +259,15 @@ def _declare(L):
                                            C.POINTER(AsdpocsScalars)]
     L.ufoir_tv_gradient.argtypes = [vp, vp, C.c_size_t, C.c_size_t, C.c_size_t, vp]
     L.ufoir_ctx_inject_copy_timeout.argtypes = [vp, C.c_int]
+    L.ufoir_ctx_set_autotune.argtypes = [vp, C.c_int]
+    L.ufoir_ctx_sm_count.argtypes = [vp]
+    L.ufoir_projector_autotune.argtypes = [vp, C.c_size_t, C.POINTER(FpTuning)]
+    L.ufoir_batch_create.argtypes = [vp, C.POINTER(BatchJob), C.c_size_t, C.POINTER(vp)]
+    L.ufoir_batch_run.argtypes = [vp, C.c_uint]
+    L.ufoir_batch_set_active.argtypes = [vp, C.c_size_t, C.c_int]
+    L.ufoir_batch_launches.argtypes = [vp, C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
+    L.ufoir_batch_destroy.argtypes = [vp]
+    L.ufoir_batch_destroy.restype = None
 
 
 class DeviceArray:
@@ -377,6 +406,12 @@ class Context:
     def __exit__(self, *exc):
         self.close()
 
+    def sm_count(self) -> int:
+        return int(lib().ufoir_ctx_sm_count(self.handle))
+
+    def set_autotune(self, on: bool):
+        self._check(lib().ufoir_ctx_set_autotune(self.handle, int(bool(on))))
+
     def l1_norm(self, v, mode=NORM_FP64) -> float:
         out = C.c_float()
         h, w = _shape(v)[-2:]
@@ -478,6 +513,13 @@ class ParallelProjector:
         n = self.params.angles_num
         return (np.ctypeslib.as_array(s, (n,)).copy(), np.ctypeslib.as_array(c, (n,)).copy())
 
+    def autotune(self, n_slices: int = 1) -> dict:
+        """Searches the forward projector's launch shapes for this geometry
+        (ufoir_projector_autotune); the geometry must be set."""
+        t = FpTuning()
+        self.ctx._check(lib().ufoir_projector_autotune(self.handle, n_slices, C.byref(t)))
+        return t.as_dict()
+
     def subsets(self):
         p = C.POINTER(Subset)()
         n = C.c_uint()
@@ -558,6 +600,54 @@ class SirtBatch:
             self.handle = None
 
 
+class Batch:
+    """A mixed SIRT batch (ufoir_batch_*): members are (DeviceArray sinogram
+    [n_angles, n_dets], DeviceArray volume [n_dets, n_dets], dict(step=...,
+    axis_position=-1, relaxation_factor=0.25, keep_vol=0))."""
+
+    def __init__(self, ctx: Context, members):
+        self.ctx = ctx
+        arr = (BatchJob * len(members))()
+        self._keep = []
+        for k, (sino, vol, kw) in enumerate(members):
+            na, n = sino.shape[-2:]
+            arr[k].n_dets = n
+            arr[k].n_angles = na
+            arr[k].step = float(np.float32(kw["step"]))
+            arr[k].axis_position = float(kw.get("axis_position", -1.0))
+            arr[k].relaxation_factor = float(kw.get("relaxation_factor", 0.25))
+            arr[k].sino = sino.ptr
+            arr[k].vol = vol.ptr
+            arr[k].keep_vol = int(kw.get("keep_vol", 0))
+            arr[k].arithmetic = int(kw.get("arithmetic", ARITH_EXACT))
+            self._keep.append((sino, vol))
+        h = C.c_void_p()
+        ctx._check(lib().ufoir_batch_create(ctx.handle, arr, len(members), C.byref(h)))
+        self.handle = h.value
+
+    def run(self, iterations: int = 1):
+        self.ctx._check(lib().ufoir_batch_run(self.handle, iterations))
+
+    def set_active(self, member: int, active: bool):
+        self.ctx._check(lib().ufoir_batch_set_active(self.handle, member, int(bool(active))))
+
+    def launches(self):
+        a, b = C.c_uint(), C.c_uint()
+        self.ctx._check(lib().ufoir_batch_launches(self.handle, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if self.handle:
+            lib().ufoir_batch_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 def sart(proj, sino, vol=None, **kw):
     return _run_method("sart", proj, sart_params(**kw), sino, vol)
 
@@ -620,12 +710,13 @@ class Server:
 
     def __init__(self, ctx: Context, hbm_budget: int = 0, max_active_jobs: int = 0,
                  policy: int = SERVE_CONTINUOUS, quantum: int = 1, fail_allocation_every: int = 0,
-                 max_running: int = 0, admit_age_ms: int = 0):
+                 max_running: int = 0, admit_age_ms: int = 0, batch_sirt: bool = True):
         self.ctx = ctx
         cfg = ServeConfig()
         lib().ufoir_serve_config_init(C.byref(cfg))
         if admit_age_ms:
             cfg.admit_age_ms = admit_age_ms
+        cfg.batch_sirt = int(bool(batch_sirt))
         cfg.hbm_budget_bytes = hbm_budget
         if max_active_jobs:
             cfg.max_active_jobs = max_active_jobs
