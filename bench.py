@@ -285,6 +285,8 @@ def run_ufoir(args, dist):
     step = float(np.float32(np.pi / na))
     proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=0)
     d_sino, d_vol, noisy = make_inputs(ufoir, ctx, proj, dist.rank, S)
+    if args.arithmetic == "fast":
+        proj.set(arithmetic=ufoir.ARITH_FAST)
 
     batch = ufoir.SirtBatch(proj, d_sino, d_vol, relaxation_factor=RELAX)
     for _ in range(max(args.warmup, 0)):
@@ -367,6 +369,8 @@ def run_ufoir(args, dist):
                        "packed-FP32 sequence from shared memory on every SM)" % ("" if dom == "fp" else "_bp")}
     roofline["fma_pipe_bound"] = fma_pipe_bound(dom, dom_rate, sm_count, clock_info, fast=False)
 
+    if args.arithmetic == "fast":
+        roofline["fma_pipe_bound"] = fma_pipe_bound(dom, dom_rate, sm_count, clock_info, fast=True)
     out = {"metric": METRIC, "value": value, "unit": "slice-iters/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -377,7 +381,8 @@ def run_ufoir(args, dist):
                       "slices_per_gpu": S, "n_dets": n, "n_angles": na, "relaxation_factor": RELAX,
                       "step": "one SIRT iteration over all slices, one CUDA graph (pad+transpose, FP, BP)",
                       "l2": "inputs larger than L2 (about 3 GB resident working set per GPU)",
-                      "parallelism": "replicas: slices sharded across ranks, no collective"},
+                      "parallelism": "replicas: slices sharded across ranks, no collective",
+                      "arithmetic": args.arithmetic},
            "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "roofline": roofline,
            "kernel_ms": kernel_ms, "sample_rate": sample_rate,
            **{k: v for k, v in per_job.items() if not k.startswith("_")}}
@@ -810,6 +815,8 @@ def main():
                     help="also time one call of each other configured method workload (C1, C2, C3a/b, C4)")
     ap.add_argument("--projector-models", action="store_true",
                     help="only time the Joseph and Siddon projectors on one resident 1448^2 x 1200 slice")
+    ap.add_argument("--arithmetic", default="exact", choices=["exact", "fast"],
+                    help="interpolation arithmetic of the headline's projector (exact = the reference's rounding)")
     ap.add_argument("--mixed-batch", action="store_true",
                     help="only the mixed-batch comparison (per-job vs one batch of uneven SIRT jobs)")
     args = ap.parse_args()

@@ -129,6 +129,10 @@ int ufoir_projector_set_params(ufoir_projector *proj, const ufoir_projector_para
     int rc = check_params(proj->ctx, &q);
     if (rc)
         return rc;
+    /* a tuned launch shape belongs to the axis and arithmetic it was timed
+     * with (the tile lists stay: graphs captured earlier may refer to them) */
+    if (q.axis_position != proj->prm.axis_position || q.arithmetic != proj->prm.arithmetic)
+        proj->fp_cfg_valid = 0;
     proj->prm = q;
     return UFOIR_OK;
 }
