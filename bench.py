@@ -322,6 +322,8 @@ def run_ufoir(args, dist):
     mixed = None
     if not args.quick and dist.rank == 0:
         mixed = mixed_batch_section(ufoir, ctx)
+        mixed["small_jobs"] = mixed_batch_section(ufoir, ctx, sizes=SERVE_SIZES[:2], n_jobs=32, max_angles=600,
+                                                  seed=MIX_SEED + 1)
     methods = methods_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
     models = projector_models_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
 
@@ -599,7 +601,7 @@ MIX_ITERS = 20
 MIX_SEED = 6006
 
 
-def mixed_batch_section(ufoir, ctx):
+def mixed_batch_section(ufoir, ctx, sizes=None, n_jobs=None, max_angles=1800, seed=None):
     """A mix of one-slice SIRT jobs of uneven size (grid n in {367, 724, 1448,
     2900}, angles U{90..1800}, seeded), each advanced MIX_ITERS iterations,
     all data resident in HBM, three ways on the same GPU:
@@ -614,23 +616,26 @@ def mixed_batch_section(ufoir, ctx):
     iteration); each member's result equals its per-job result bit for bit
     (tests/test_gpu_batch.py)."""
     from ufoir import synth
-    rng = np.random.default_rng(MIX_SEED)
+    sizes = sizes or SERVE_SIZES
+    n_jobs = n_jobs or MIX_JOBS
+    seed = seed or MIX_SEED
+    rng = np.random.default_rng(seed)
     jobs, cache = [], {}
-    for i in range(MIX_JOBS):
-        P, n = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
-        na = int(rng.integers(90, 1801))
+    for i in range(n_jobs):
+        P, n = sizes[int(rng.integers(len(sizes)))]
+        na = int(rng.integers(90, max_angles + 1))
         step = float(np.float32(np.pi / na))
         if n not in cache:
-            cache[n] = synth.ellipse_phantom(n, P, 10, seed=MIX_SEED + n)
+            cache[n] = synth.ellipse_phantom(n, P, 10, seed=seed + n)
         proj = ufoir.ParallelProjector(ctx, step=step, angles_num=na, is_forward=1)
         clean = proj.forward(cache[n], np.zeros((na, n), np.float32))
         proj.close()
-        sino, _ = synth.poisson_noise(clean, I0, seed=MIX_SEED + i)
+        sino, _ = synth.poisson_noise(clean, I0, seed=seed + i)
         jobs.append((n, na, step, ufoir.DeviceArray.from_numpy(ctx, sino), ufoir.DeviceArray(ctx, (n, n), zero=True)))
     samples = float(sum(2.0 * n * n * na for n, na, *_ in jobs)) * MIX_ITERS
-    slice_iters = MIX_JOBS * MIX_ITERS
-    out = {"workload": f"{MIX_JOBS} one-slice SIRT jobs, grid n in {{367,724,1448,2900}}, angles U{{90..1800}} "
-                       f"(seed {MIX_SEED}), {MIX_ITERS} iterations each, data resident in HBM",
+    slice_iters = n_jobs * MIX_ITERS
+    out = {"workload": f"{n_jobs} one-slice SIRT jobs, grid n in {{{','.join(str(n) for _, n in sizes)}}}, angles "
+                       f"U{{90..{max_angles}}} (seed {seed}), {MIX_ITERS} iterations each, data resident in HBM",
            "jobs": [[n, na] for n, na, *_ in jobs], "samples": samples}
 
     def rate(sec):
@@ -708,29 +713,26 @@ METHOD_CPU = ("sart", "sirt", "asdpocs", "sbtv")
 
 
 def method_cpu_baseline(method, n, na, step, sino, kw):
-    """The oracle port (the reference's kernels and host loop restated in C,
-    OpenMP over the NDRange) on the first slice of a method workload, the same
-    call as the GPU's, on all host cores."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    pyoracle.build()
-    threads = os.cpu_count() or 1
-    pyoracle.set_threads(threads)
+    """The reference's CPU path on the first slice of a method workload, the
+    same call as the GPU's, on all host cores: its OpenCL kernels compiled for
+    the host (oracle/_ref) driven by the oracle's host loop (the C port where
+    the kernel sources are absent)."""
+    pyoracle, threads, which = _cpu_oracle()
     p = pyoracle.projector(n, na, step)
     sino = np.ascontiguousarray(sino, np.float32)
     t0 = time.perf_counter()
     if method == "sart":
-        pyoracle.sart(p, sino, kw["num_iterations"], 0.25)
+        pyoracle.sart(p, sino, kw["num_iterations"], 0.25, which=which)
     elif method == "sirt":
-        pyoracle.sirt(p, sino, kw["num_iterations"], 0.25)
+        pyoracle.sirt(p, sino, kw["num_iterations"], 0.25, which=which)
     elif method == "sbtv":
         pyoracle.sbtv(p, sino, pyoracle.sbtv_params(num_iterations=kw["num_iterations"], lambda_=kw["lambda"],
-                                                    mu=kw["mu"], norm_mode=pyoracle.NORM_FP64))
+                                                    mu=kw["mu"], norm_mode=pyoracle.NORM_FP64), which=which)
     else:
         pyoracle.asdpocs(p, sino, pyoracle.asdpocs_params(num_iterations=kw["num_iterations"],
-                                                         norm_mode=pyoracle.NORM_FP64))
+                                                         norm_mode=pyoracle.NORM_FP64), which=which)
     dt = time.perf_counter() - t0
-    return {"ms_per_call": dt * 1e3, "cores": threads, "kind": "port", "sample": "the whole call, slice 0"}
+    return {"ms_per_call": dt * 1e3, "cores": threads, "kind": _cpu_kind(which), "sample": "the whole call, slice 0"}
 
 
 def methods_section(ufoir, ctx):
@@ -829,7 +831,10 @@ def main():
     if args.mixed_batch:
         import ufoir
         ctx = ufoir.Context(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps(mixed_batch_section(ufoir, ctx)), flush=True)
+        out = mixed_batch_section(ufoir, ctx)
+        out["small_jobs"] = mixed_batch_section(ufoir, ctx, sizes=SERVE_SIZES[:2], n_jobs=32, max_angles=600,
+                                                seed=MIX_SEED + 1)
+        print(json.dumps(out), flush=True)
         ctx.close()
         return
     dist = Dist()

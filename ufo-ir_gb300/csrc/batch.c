@@ -348,8 +348,26 @@ int ufoir__batch_build(ufoir_ctx *ctx, const ufoir__bmember *mem, int n, ufoir_b
     if (!b)
         return ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
     int rc = UFOIR_OK;
+    /* as in ufoir_batch_create: shapes for a full GPU when the members'
+     * tiles fill it twice over */
+    const int sm = udev_sm_count(ctx->dev);
+    long long total = 0;
+    for (int i = 0; i < n && !rc; i++) {
+        const int A = udev_fp_tile_angles(ctx->dev, (int) mem[i].p->n_dets);
+        int nt = 0;
+        if (A > 0)
+            rc = ufoir__projector_tiles(mem[i].p, A, NULL, &nt, NULL);
+        total += nt;
+        b->m[i].cost = (double) nt;       /* tiles, until the cost below */
+    }
     for (int i = 0; i < n && !rc; i++) {
         member *m = &b->m[i];
+        const int nt = (int) m->cost;
+        int slices = mem[i].shape_slices;
+        if (total >= 2LL * sm && nt > 0) {
+            const int fill = (2 * sm + nt - 1) / nt;
+            slices = slices > fill ? slices : fill;
+        }
         m->p = mem[i].p;
         m->b = mem[i].b;
         m->x = mem[i].x;
@@ -360,7 +378,7 @@ int ufoir__batch_build(ufoir_ctx *ctx, const ufoir__bmember *mem, int n, ufoir_b
         m->TP = mem[i].TP;
         m->lambda = mem[i].lambda;
         m->cost = 2.0 * (double) m->p->n_dets * (double) m->p->n_dets * (double) m->p->n_angles;
-        rc = member_shape(ctx, m, mem[i].shape_slices);
+        rc = member_shape(ctx, m, slices);
     }
     if (!rc)
         rc = build_lists(b);
