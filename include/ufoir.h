@@ -104,10 +104,11 @@ UFOIR_API uint64_t ufoir_ctx_kernel_launches(const ufoir_ctx *ctx);
 UFOIR_API int ufoir_ctx_timer_begin(ufoir_ctx *ctx);
 /* Testing the device-side bounded waits (no reference counterpart; the
  * reference logs OpenCL errors and continues, src/core/ufo-ir-basic-ops.c:60-64):
- * the next tiled forward projection launched on this context leaves the
- * shared-memory bulk copy of row chunk `chunk` unissued in every CTA (-1
- * cancels). Its waits then run out after their 250 ms limit, the kernel
- * drains its other copies, writes nothing and records the timeout, and the
+ * in the next tiled forward projection launched on this context, the
+ * shared-memory barrier of row chunk `chunk` expects 16 bytes more than the
+ * chunk's bulk copy brings, in every CTA (-1 cancels), so it never completes.
+ * Its waits then run out after their 250 ms limit, the kernel drains its
+ * copies (all of which land), writes nothing and records the timeout, and the
  * call returns UFOIR_ERR_TIMEOUT; the context stays usable. One-shot. */
 UFOIR_API int ufoir_ctx_inject_copy_timeout(ufoir_ctx *ctx, int chunk);
 UFOIR_API int ufoir_ctx_timer_end(ufoir_ctx *ctx, float *ms);

@@ -5,8 +5,9 @@ The tiled forward projector stages image rows in shared memory with bulk
 copies tracked by mbarriers; every wait on them gives up after 250 ms,
 records the timeout in the kernel error word, drains the copies it issued
 and returns, and the host turns the word into UFOIR_ERR_TIMEOUT. Here the
-host asks one launch to leave one chunk's copy unissued
-(ufoir_ctx_inject_copy_timeout), so every CTA's wait on it runs out. The call
+host asks one launch to announce more bytes for one chunk's barrier than its
+copy brings (ufoir_ctx_inject_copy_timeout), so the barrier never completes
+and every CTA's wait on it runs out. The call
 must fail with UFOIR_ERR_TIMEOUT within seconds, and the same context must
 then give the oracle's result bit for bit. (The reference only logs OpenCL
 errors and continues, src/core/ufo-ir-basic-ops.c:60-64.)

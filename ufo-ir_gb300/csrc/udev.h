@@ -181,8 +181,8 @@ int udev_memset(udev *d, void *p, int value, size_t bytes);
 /* Returns UFOIR_ERR_TIMEOUT (and clears the word) if a kernel recorded a
  * bounded-wait timeout since the last check; waits for the stream. */
 int udev_take_kernel_error(udev *d);
-/* Testing: the next tiled forward projection launch leaves the bulk copy of
- * row chunk `chunk` unissued in every CTA (-1 = none). */
+/* Testing: in the next tiled forward projection launch, the barrier of row
+ * chunk `chunk` never completes in any CTA (-1 = none). */
 void udev_inject_copy_skip(udev *d, int chunk);
 
 /* The "siddon" model (udev_siddon.cu): exact line integrals of the pixel

@@ -67,7 +67,7 @@ struct FpTileArgs {
     int wcols;             /* columns staged per row: pitch (whole rows), or a window of the CTA's rays */
     int wstride;           /* shared floats per staged row (wcols + 4 for windows: 2 zero slots) */
     int margin;            /* window margin in columns (the recurrence's drift and the filter's taps) */
-    int skip_chunk;        /* testing: row chunk whose copy is left unissued (-1 = none) */
+    int skip_chunk;        /* testing: row chunk whose barrier never completes (-1 = none) */
     int *err;
 };
 
@@ -185,19 +185,20 @@ __device__ __forceinline__ void fp_tile(const FpTileArgs &P, int tile_idx, int d
     auto issue = [&](int ch) {
         const int r0 = ch * K, rows = min(K, n - r0);
         float *dst = stage0 + (ch & 1) * stage_floats;
-        /* testing (ufoir_ctx_inject_copy_timeout): leave this chunk's copy
-         * unissued, so that its waits run out and the error path runs */
-        if (ch == P.skip_chunk)
-            return;
+        /* testing (ufoir_ctx_inject_copy_timeout): the barrier of chunk
+         * skip_chunk expects 16 bytes more than its copies bring, so its
+         * phase never completes, its waits run out and the error path runs.
+         * (Written as arithmetic: a branch here cost the kernel 5 %.) */
+        const uint32_t extra = ch == P.skip_chunk ? 16u : 0u;
         if (!win) {
             const uint32_t bytes = (uint32_t) (rows * pitch) * 4u;
             w0s[ch & 1] = 0;
-            tma::mbar_arrive_expect_tx(&bars[ch & 1], bytes);
+            tma::mbar_arrive_expect_tx(&bars[ch & 1], bytes + extra);
             tma::bulk_g2s(dst, img + (size_t) r0 * pitch, bytes, &bars[ch & 1]);
         } else {
             const int w0 = window(r0, rows);
             w0s[ch & 1] = w0;
-            tma::mbar_arrive_expect_tx(&bars[ch & 1], (uint32_t) (rows * wcols) * 4u);
+            tma::mbar_arrive_expect_tx(&bars[ch & 1], (uint32_t) (rows * wcols) * 4u + extra);
             for (int r = 0; r < rows; ++r)
                 tma::bulk_g2s(dst + (size_t) r * wstride, img + (size_t) (r0 + r) * pitch + w0,
                               (uint32_t) wcols * 4u, &bars[ch & 1]);
