@@ -510,9 +510,17 @@ int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_job
         geo_count[g]++;
     }
     UFOIR_TRY(shape_slices(ctx, b->projs, geo_count, b->n_projs, geo_eff));
+    /* With autotune on, each geometry's shape is searched; in a batch a
+     * tuned shape that differs from the fixed rules' adds a launch unless
+     * other members share it, and the search times each geometry alone, so
+     * a tuned shape is kept only where it wins by at least 10 %. */
     if (ctx->autotune)
-        for (int g = 0; g < b->n_projs; g++)
-            UFOIR_TRY(ufoir__fp_tune(b->projs[g], geo_eff[g], NULL));
+        for (int g = 0; g < b->n_projs; g++) {
+            ufoir_fp_tuning t;
+            UFOIR_TRY(ufoir__fp_tune(b->projs[g], geo_eff[g], &t));
+            if (t.tuned && !(t.ms_tuned < 0.9f * t.ms_default))
+                b->projs[g]->fp_cfg_valid = 0;
+        }
     for (int i = 0; i < n; i++) {
         const ufoir_batch_job *j = &jobs[i];
         member *m = &b->m[i];
