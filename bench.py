@@ -545,9 +545,9 @@ def serve_trace(ufoir, ctx, n_jobs):
     return jobs, samples
 
 
-def run_serve(ufoir, ctx, jobs, policy):
+def run_serve(ufoir, ctx, jobs, policy, batch_sirt=False):
     """Submits the trace at its arrival times from one host thread and waits for all jobs."""
-    with ufoir.Server(ctx, hbm_budget=SERVE_BUDGET, policy=policy) as srv:
+    with ufoir.Server(ctx, hbm_budget=SERVE_BUDGET, policy=policy, batch_sirt=batch_sirt) as srv:
         t0 = time.perf_counter()
         ids = []
         for (t, desc, sino, *_rest) in jobs:
@@ -585,11 +585,12 @@ def serve_section(ufoir, ctx, n_jobs):
                               ("asdpocs", ufoir.METHOD_ASDPOCS))}}}
     keys = ("completed", "failed", "p50_latency_ms", "p99_latency_ms", "mean_latency_ms", "max_latency_ms",
             "p50_queue_ms", "p99_queue_ms", "throughput_jobs_per_s", "busy_seconds", "peak_hbm_bytes",
-            "peak_active_jobs", "wall_s")
-    for name, pol in (("one_at_a_time", ufoir.SERVE_ONE_AT_A_TIME),
-                      ("sjf_one_at_a_time", ufoir.SERVE_SJF_ONE_AT_A_TIME),
-                      ("continuous", ufoir.SERVE_CONTINUOUS)):
-        st = run_serve(ufoir, ctx, jobs, pol)
+            "peak_active_jobs", "wall_s", "batched_iterations")
+    for name, pol, bs in (("one_at_a_time", ufoir.SERVE_ONE_AT_A_TIME, False),
+                          ("sjf_one_at_a_time", ufoir.SERVE_SJF_ONE_AT_A_TIME, False),
+                          ("continuous", ufoir.SERVE_CONTINUOUS, False),
+                          ("continuous_batched_sirt", ufoir.SERVE_CONTINUOUS, True)):
+        st = run_serve(ufoir, ctx, jobs, pol, bs)
         out[name] = {k: st[k] for k in keys if k in st}
         out[name]["samples_per_s"] = samples / st["busy_seconds"] if st.get("busy_seconds") else None
     return out

@@ -451,9 +451,11 @@ typedef struct {
                                          with the least remaining work first; 0 = 4 */
     unsigned int admit_age_ms;        /* CONTINUOUS: how long a queued job that does not fit the
                                          budget may be passed by later jobs; 0 = 2000 */
-    unsigned int batch_sirt;          /* CONTINUOUS: 1 (default) = the SIRT jobs the tiled projectors
-                                         serve advance together, one mixed batch (ufoir_batch) of
-                                         the idle ones per quantum; 0 = each on its own graph */
+    unsigned int batch_sirt;          /* CONTINUOUS: 1 = the SIRT jobs the tiled projectors serve
+                                         advance together, one mixed batch (ufoir_batch) of the idle
+                                         ones per quantum: more throughput for many small jobs, but a
+                                         small job then waits for the biggest member's iteration every
+                                         quantum; 0 (default) = each on its own graph */
 } ufoir_serve_config;
 
 typedef struct {

@@ -103,7 +103,7 @@ void ufoir_serve_config_init(ufoir_serve_config *c)
     c->quantum = 1;
     c->max_running = DEFAULT_MAX_RUNNING;
     c->admit_age_ms = DEFAULT_ADMIT_AGE_MS;
-    c->batch_sirt = 1;
+    c->batch_sirt = 0;
 }
 
 void ufoir_job_desc_init(ufoir_job_desc *j)

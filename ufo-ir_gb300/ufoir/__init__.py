@@ -710,7 +710,7 @@ class Server:
 
     def __init__(self, ctx: Context, hbm_budget: int = 0, max_active_jobs: int = 0,
                  policy: int = SERVE_CONTINUOUS, quantum: int = 1, fail_allocation_every: int = 0,
-                 max_running: int = 0, admit_age_ms: int = 0, batch_sirt: bool = True):
+                 max_running: int = 0, admit_age_ms: int = 0, batch_sirt: bool = False):
         self.ctx = ctx
         cfg = ServeConfig()
         lib().ufoir_serve_config_init(C.byref(cfg))
