@@ -317,6 +317,7 @@ struct SartFpArgs {
 
 constexpr int kFpCluster = 8;                       /* CTAs per ray group at most (portable cluster) */
 constexpr int kFpLocal = kMaxBlocks / kFpCluster;   /* blocks per CTA at most */
+constexpr int kRemoteBatch = 16;                    /* block sums read over DSMEM per round */
 
 /* Programmatic dependent launch: let the next kernel in the stream launch
  * now, and wait here until the previous one has completed and its writes are
@@ -491,17 +492,24 @@ __global__ void __launch_bounds__(32 * W, MINB) sart_fp_kernel(SartFpArgs P)
         float result = src_v;
         const joseph::AxisConsts kc = joseph::axis_consts(n, P.axis);
         if (!joseph::detector_inactive(kc, sr)) {
-            /* block sums in block order; eight remote loads in flight at a time */
+            /* block sums in block order, 16 remote loads in flight at a time;
+             * block j sits on CTA j mod C in slot j / C, stepped without a
+             * division (on this path after the barrier, a division per block
+             * cost more than the loads) */
             float detected = 0.0f;
-            for (int j0 = 0; j0 < nb; j0 += 8) {
-                float bsv[8];
+            int rk = 0, slot = 0;
+            for (int j0 = 0; j0 < nb; j0 += kRemoteBatch) {
+                float bsv[kRemoteBatch];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const int j = min(j0 + k, nb - 1);
-                    bsv[k] = ld_cluster(&bs_local[j / C][threadIdx.x], j % C);
+                for (int k = 0; k < kRemoteBatch; ++k) {
+                    bsv[k] = j0 + k < nb ? ld_cluster(&bs_local[slot][threadIdx.x], rk) : 0.0f;
+                    if (++rk == C) {
+                        rk = 0;
+                        ++slot;
+                    }
                 }
 #pragma unroll
-                for (int k = 0; k < 8; ++k)
+                for (int k = 0; k < kRemoteBatch; ++k)
                     if (j0 + k < nb)
                         detected = __fadd_rn(detected, bsv[k]);
             }
@@ -1028,9 +1036,9 @@ extern "C" int udev_sart_bp(udev *d, const udev_geom *g, int angle, float sn, fl
     A.err = d->d_err;
     A.vol_stride = (long long) plane;
     A.sino_stride = (long long) g->n_angles * n;
-    /* 32-row tiles while they leave fewer than ~4 CTAs per SM, else 64-row */
-    const bool tall = (long long) udev_div_up(n, kBpTileW) * udev_div_up(n, 64) * n_slices >= 4LL * udev_sm_count(d);
-    dim3 grid(udev_div_up(n, kBpTileW), udev_div_up(n, tall ? 64 : 32), (unsigned int) n_slices);
+    /* 32-row tiles at every size: at 2900^2 they took 1 us off each angle against
+     * 64-row tiles (2.3 waves of those at three CTAs per SM left a thin last wave) */
+    dim3 grid(udev_div_up(n, kBpTileW), udev_div_up(n, 32), (unsigned int) n_slices);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = dim3(32, 8, 1);
@@ -1040,10 +1048,8 @@ extern "C" int udev_sart_bp(udev *d, const udev_geom *g, int angle, float sn, fl
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = sart_pdl(d, n, n_slices) ? 1 : 0;
-    const cudaError_t e = tall ? (place == 1 ? cudaLaunchKernelEx(&cfg, sart_bp_kernel<true, 8>, A)
-                                             : cudaLaunchKernelEx(&cfg, sart_bp_kernel<false, 8>, A))
-                               : (place == 1 ? cudaLaunchKernelEx(&cfg, sart_bp_kernel<true, 4>, A)
-                                             : cudaLaunchKernelEx(&cfg, sart_bp_kernel<false, 4>, A));
+    const cudaError_t e = place == 1 ? cudaLaunchKernelEx(&cfg, sart_bp_kernel<true, 4>, A)
+                                     : cudaLaunchKernelEx(&cfg, sart_bp_kernel<false, 4>, A);
     if (e != cudaSuccess) {
         cudaGetLastError();
         udev_set_error(d, "sart_bp_kernel launch: %s", cudaGetErrorString(e));
