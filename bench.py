@@ -46,6 +46,7 @@ sys.path.insert(0, os.path.join(ROOT, "ufo-ir_gb300"))
 METRIC = "SIRT slice-iters/s @1024²×1200 ang; serve p50/p99 latency vs plain per-job path"
 N_DETS, N_ANGLES, PHANTOM, SLICES, I0, RELAX = 1448, 1200, 1024, 64, 1e5, 0.25
 E2E_ITERS = 10
+E2E_CALLS = 3
 # serve trace: the configured request mix (job shapes, methods, iteration
 # counts, arrival rate, budget) with its first SERVE_JOBS jobs
 SERVE_JOBS = 12
@@ -324,7 +325,7 @@ def run_ufoir(args, dist):
         mixed = mixed_batch_section(ufoir, ctx)
         mixed["small_jobs"] = mixed_batch_section(ufoir, ctx, sizes=SERVE_SIZES[:2], n_jobs=32, max_angles=600,
                                                   seed=MIX_SEED + 1)
-    methods = methods_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
+    methods = methods_section(ufoir, ctx, cpu=not args.no_cpu_baseline) if args.methods and dist.rank == 0 else None
     models = projector_models_section(ufoir, ctx) if args.methods and dist.rank == 0 else None
 
     # roofline of the dominant kernel (live CUDA-event durations above)
@@ -482,14 +483,20 @@ def end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S):
     h_sino[...] = noisy
     h_vol = ctx.pinned_empty((S, n, n))
     ufoir.sirt(proj, h_sino, h_vol, num_iterations=1, relaxation_factor=RELAX)   # warm
-    dist.barrier()
-    t0 = time.perf_counter()
-    ufoir.sirt(proj, h_sino, h_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
-    e2e_s = dist.max(time.perf_counter() - t0)
+    # three timed calls, the median reported: single host-buffer calls of the same
+    # work were seen to vary by up to 6 % between otherwise identical runs
+    calls = []
+    for _ in range(E2E_CALLS):
+        dist.barrier()
+        t0 = time.perf_counter()
+        ufoir.sirt(proj, h_sino, h_vol, num_iterations=E2E_ITERS, relaxation_factor=RELAX)
+        calls.append(dist.max(time.perf_counter() - t0))
+    e2e_s = sorted(calls)[len(calls) // 2]
     e2e = {"value": S * E2E_ITERS * dist.world / e2e_s, "unit": "slice-iters/s",
            "h2d_bytes_per_step": int(h_sino.nbytes), "d2h_bytes_per_step": int(h_vol.nbytes),
-           "call": f"ufoir_sirt_process(host buffers, {S} slices, num-iterations {E2E_ITERS})",
-           "seconds": e2e_s}
+           "call": f"ufoir_sirt_process(host buffers, {S} slices, num-iterations {E2E_ITERS}), "
+                   f"median of {E2E_CALLS} calls",
+           "seconds": e2e_s, "seconds_each_call": calls}
 
     # one job per launch sequence (plain per-job path) vs the batched call, same API, device data
     jobs = 8
@@ -736,9 +743,10 @@ def method_cpu_baseline(method, n, na, step, sino, kw):
     return {"ms_per_call": dt * 1e3, "cores": threads, "kind": _cpu_kind(which), "sample": "the whole call, slice 0"}
 
 
-def methods_section(ufoir, ctx):
+def methods_section(ufoir, ctx, cpu=True):
     """One call of each other configured method workload on one slice,
-    resident in HBM: the call time (after one untimed call) and its rate."""
+    resident in HBM: the call time (after one untimed call) and its rate;
+    with cpu, the reference's CPU path on the same call beside it."""
     from ufoir import synth
     out = []
     for name, method, n, na, P, kind, i0, S, kw in METHOD_CASES:
@@ -762,7 +770,7 @@ def methods_section(ufoir, ctx):
         iters = kw["num_iterations"]
         row = {"workload": name, "slices": S, "ms_per_call": ms, "ms_per_iteration": ms / iters,
                "ms_per_slice_iteration": ms / iters / S, "samples_per_slice_iteration_fp_bp": 2.0 * n * n * na}
-        if method in METHOD_CPU:
+        if cpu and method in METHOD_CPU:
             row["cpu_baseline"] = method_cpu_baseline(method, n, na, np.float32(step), sino[0], kw)
         out.append(row)
         proj.close()
@@ -807,7 +815,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ufoir", choices=["ufoir", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU baselines (the headline's and, with --methods, each method's)")
     ap.add_argument("--slices", type=int, default=SLICES, help="slices per GPU (64 = the headline workload)")
     ap.add_argument("--quick", action="store_true",
                     help="only the resident timed steps (skip e2e, per-job comparison, serve trace, CPU baseline)")
