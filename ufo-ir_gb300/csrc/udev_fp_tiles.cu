@@ -547,7 +547,8 @@ static int kernels_init_fm(udev *d)
 int udev_kernels_init(udev *d)
 {
     int rc = kernels_init_fm<false>(d);
-    return rc ? rc : kernels_init_fm<true>(d);
+    rc = rc ? rc : kernels_init_fm<true>(d);
+    return rc ? rc : udev_sart_init(d);
 }
 
 extern "C" int udev_pad_transpose(udev *d, const float *vol, float *volP, float *volTP, int n, int n_slices)

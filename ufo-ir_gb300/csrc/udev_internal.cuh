@@ -29,10 +29,14 @@ struct udev {
     int *d_err = nullptr;           /* kernel error word (bounded-wait timeouts) */
     int *h_err = nullptr;
     int inject_skip_chunk = -1;     /* testing: see udev_inject_copy_skip */
+    int sart_wide_clusters = 0;     /* 16-CTA clusters of the segment-form SART FP that fit at once */
 };
 
 /* One-time kernel attribute setup (dynamic shared memory opt-in). */
 int udev_kernels_init(udev *d);
+
+/* The same for the SART per-angle kernels (non-portable cluster sizes). */
+int udev_sart_init(udev *d);
 
 #define UDEV_BIND(d)                                                                   \
     do {                                                                               \

@@ -317,6 +317,7 @@ struct SartFpArgs {
 };
 
 constexpr int kFpCluster = 8;                       /* CTAs per ray group at most (portable cluster) */
+constexpr int kFpWideCluster = 16;                  /* the same, non-portable, for the segment form */
 constexpr int kFpLocal = kMaxBlocks / kFpCluster;   /* blocks per CTA at most */
 constexpr int kRemoteBatch = 16;                    /* block sums read over DSMEM per round */
 constexpr size_t kPrefetchTableBytes = (size_t) 64 << 20;   /* block-start tables above this are prefetched */
@@ -756,6 +757,35 @@ __global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
 
 }  // namespace
 
+/* Lets the segment-form FP run in clusters of 16 CTAs and counts how many
+ * such clusters fit on this GPU at once (0 where the size is refused). */
+int udev_sart_init(udev *d)
+{
+    const void *func = (const void *) sart_fp_kernel<4, 16, 4, 3>;
+    d->sart_wide_clusters = 0;
+    if (cudaFuncSetAttribute(func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return UFOIR_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned int) kFpWideCluster, 1, 1);
+    cfg.blockDim = dim3(128, 1, 1);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned int) kFpWideCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, func, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        clusters = 0;
+    }
+    d->sart_wide_clusters = clusters;
+    return UFOIR_OK;
+}
+
 extern "C" size_t udev_fp_block_starts_floats(int n, int n_angles)
 {
     const int nb = (n + kBlock - 1) / kBlock;
@@ -916,7 +946,12 @@ static SartFpShape sart_fp_shape(udev *d, int n, int n_slices)
     const int nb = (n + kBlock - 1) / kBlock, groups = (n + 63) / 64;
     const long long sms = udev_sm_count(d);
     SartFpShape f;
-    if (nb <= 2 * kFpCluster) {
+    if (nb > kFpCluster && nb <= 2 * kFpWideCluster && (long long) groups * n_slices <= d->sart_wide_clusters) {
+        /* one or two blocks per CTA over a non-portable cluster of up to 16
+         * CTAs, where every ray group's cluster fits on the GPU at once */
+        f.shape = 0;
+        f.cluster = nb < kFpWideCluster ? nb : kFpWideCluster;
+    } else if (nb <= 2 * kFpCluster) {
         f.shape = 0;
         f.cluster = nb < kFpCluster ? nb : kFpCluster;
     } else if (udev_div_up(nb, 4) <= kFpCluster && (long long) groups * udev_div_up(nb, 4) * n_slices <= 3 * sms) {
