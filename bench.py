@@ -483,8 +483,9 @@ def end_to_end(ufoir, ctx, proj, d_sino, d_vol, noisy, dist, S):
     h_sino[...] = noisy
     h_vol = ctx.pinned_empty((S, n, n))
     ufoir.sirt(proj, h_sino, h_vol, num_iterations=1, relaxation_factor=RELAX)   # warm
-    # three timed calls, the median reported: single host-buffer calls of the same
-    # work were seen to vary by up to 6 % between otherwise identical runs
+    # three timed calls, the median reported: host copies that follow a long
+    # GPU phase were measured at 11-70 GB/s on the GB300 machine against 190-210
+    # GB/s back to back, so single calls of the same work vary by a few %
     calls = []
     for _ in range(E2E_CALLS):
         dist.barrier()

@@ -28,6 +28,38 @@ def _method_proj(ufoir, ctx, step, axis=-1.0):
     return ufoir.ParallelProjector(ctx, step=float(step), axis_position=float(axis), is_forward=0)
 
 
+# ufoir_sirt_process splits the first and last iterations into slice chunks
+# where they meet host data (sinograms arriving, volumes leaving on a side
+# stream). Every mix of host and device buffers, slice counts that split
+# unevenly and iteration counts 1-3 must give the device path's values, and
+# the oracle's.
+@pytest.mark.parametrize("slices,iters", [(1, 1), (3, 2), (5, 3), (6, 1), (7, 2)])
+@pytest.mark.parametrize("sino_on_host,vol_on_host", [(True, True), (True, False), (False, True)])
+def test_sirt_host_buffers_split_iterations(ufoir_lib, gpu_ctx, oracle, slices, iters, sino_on_host,
+                                            vol_on_host):
+    n, na = 72, 45
+    step = np.float32(np.pi / na)
+    sinos = np.random.default_rng(slices * 10 + iters).random((slices, na, n), dtype=np.float32) * n
+    p = _method_proj(ufoir_lib, gpu_ctx, step)
+    d_s = ufoir_lib.DeviceArray.from_numpy(gpu_ctx, sinos)
+    d_v = ufoir_lib.DeviceArray(gpu_ctx, (slices, n, n), zero=True)
+    ufoir_lib.sirt(p, d_s, d_v, num_iterations=iters, relaxation_factor=0.25)
+    want_dev = d_v.download()
+    s_arg = sinos if sino_on_host else d_s
+    v_out = np.full((slices, n, n), np.nan, np.float32)
+    v_arg = v_out if vol_on_host else ufoir_lib.DeviceArray(gpu_ctx, (slices, n, n), zero=True)
+    ufoir_lib.sirt(p, s_arg, v_arg, num_iterations=iters, relaxation_factor=0.25)
+    got = v_out if vol_on_host else v_arg.download()
+    assert np.array_equal(got, want_dev)
+    for i in range(slices):
+        assert np.array_equal(got[i], oracle.sirt(oracle.projector(n, na, step), sinos[i], iters, 0.25)), i
+    if not vol_on_host:
+        v_arg.close()
+    d_s.close()
+    d_v.close()
+    p.close()
+
+
 @pytest.mark.parametrize("n,na,axis,iters,slices", [(16, 12, -1.0, 5, 1), (33, 40, 15.3, 4, 3),
                                                      (64, 90, -1.0, 3, 2), (100, 60, 48.75, 3, 1)])
 def test_sirt_matches_oracle(ufoir_lib, gpu_ctx, oracle, n, na, axis, iters, slices):

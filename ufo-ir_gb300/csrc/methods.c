@@ -183,6 +183,61 @@ int ufoir__sirt_body(void *arg)
     return rc;
 }
 
+/* Slice chunks of a SIRT call whose data cross the host boundary. */
+#define SIRT_HOST_CHUNKS 4
+
+static int sirt_chunks(int S)
+{
+    return S < SIRT_HOST_CHUNKS ? S : SIRT_HOST_CHUNKS;
+}
+
+/* First slice of chunk k of S slices in `chunks` chunks (the same split
+ * everywhere: sizes differ by at most one). */
+static int sirt_chunk_start(int S, int chunks, int k)
+{
+    return (int) (((long long) S * k) / chunks);
+}
+
+/* One SIRT iteration (the work of ufoir__sirt_body) split by slice chunks
+ * where it meets host data: with chunked_in, the forward projection of chunk
+ * k waits only for side-stream mark k (the arrival of that chunk's
+ * sinograms); with host_vol, the backprojection runs per chunk and each
+ * chunk's final volumes are copied to host_vol on the side stream while the
+ * next chunks compute. Per slice the kernels do the same work, so the values
+ * are those of the unsplit iteration. */
+static int sirt_iteration_split(ufoir__sirt_iter *s, int chunked_in, float *host_vol)
+{
+    udev *d = s->p->ctx->dev;
+    const size_t n = s->p->n_dets, nv = n * n, ns = n * s->p->n_angles;
+    const int S = s->n_slices, chunks = sirt_chunks(S);
+    int rc = UFOIR_OK;
+    if (chunked_in) {
+        for (int k = 0; k < chunks && rc == UFOIR_OK; k++) {
+            const int s0 = sirt_chunk_start(S, chunks, k), c = sirt_chunk_start(S, chunks, k + 1) - s0;
+            rc = udev_side_wait(d, k);
+            if (!rc)
+                rc = ufoir__fp_full(s->p, &s->fs, s->x + (size_t) s0 * nv, s->b + (size_t) s0 * ns, s->R, 1,
+                                    s->resid + (size_t) s0 * ns, -1.0f, c);
+        }
+    } else {
+        rc = ufoir__fp_full(s->p, &s->fs, s->x, s->b, s->R, 1, s->resid, -1.0f, S);
+    }
+    if (rc)
+        return rc;
+    if (!host_vol)
+        return udev_bp(d, &s->g, s->p->subsets, (int) s->p->n_subsets, s->resid, NULL, s->C, 1, s->x, s->x,
+                       s->lambda, S);
+    for (int k = 0; k < chunks && rc == UFOIR_OK; k++) {
+        const int s0 = sirt_chunk_start(S, chunks, k), c = sirt_chunk_start(S, chunks, k + 1) - s0;
+        float *xk = s->x + (size_t) s0 * nv;
+        rc = udev_bp(d, &s->g, s->p->subsets, (int) s->p->n_subsets, s->resid + (size_t) s0 * ns, NULL, s->C, 1,
+                     xk, xk, s->lambda, c);
+        if (!rc)
+            rc = udev_copy_after(d, host_vol + (size_t) s0 * nv, xk, (size_t) c * nv * sizeof(float));
+    }
+    return rc;
+}
+
 int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, const float *sino,
                        const size_t dims[2], float *vol, size_t n_slices)
 {
@@ -200,12 +255,25 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
     float *R = NULL, *C = NULL, *resid = NULL;
     ufoir__sirt_iter it;
     memset(&it, 0, sizeof(it));
-    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 1));
+    UFOIR_TRY(ufoir__buf_in(ctx, &bb, sino, ns * n_slices, 0));
     UFOIR_TRY(ufoir__buf_in(ctx, &bx, vol, nv * n_slices, 0));
     UFOIR_TRY(ufoir__alloc(ctx, &R, ns));
     UFOIR_TRY(ufoir__alloc(ctx, &C, nv));
     UFOIR_TRY(ufoir__alloc(ctx, &resid, ns * n_slices));
     UFOIR_TRY(ufoir__fp_scratch_alloc(proj, &it.fs, n_slices));
+    /* host sinograms move in on the side stream, chunk by chunk, while the
+     * weights are computed (they do not read b) and the first forward
+     * projection starts on the chunks that have arrived */
+    const int host_in = bb.owned, host_out = bx.owned;
+    if (host_in) {
+        const int chunks = sirt_chunks((int) n_slices);
+        UFOIR_TRY(udev_side_fence(ctx->dev));
+        for (int k = 0; k < chunks; k++) {
+            const size_t s0 = (size_t) sirt_chunk_start((int) n_slices, chunks, k);
+            const size_t s1 = (size_t) sirt_chunk_start((int) n_slices, chunks, k + 1);
+            UFOIR_TRY(udev_side_copy(ctx->dev, bb.dev + s0 * ns, sino + s0 * ns, (s1 - s0) * ns * sizeof(float), k));
+        }
+    }
 
     /* weights with relaxation 1 and correction scale 1 (sirt-task.c:176-193);
      * the output volume serves as the all-ones image before it is zeroed */
@@ -228,10 +296,26 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
     it.C = C;
     it.lambda = prm->relaxation_factor;
     it.n_slices = (int) n_slices;
-    UFOIR_TRY(run_graphed(ctx, prm->num_iterations, ufoir__sirt_body, &it));
-    UFOIR_TRY(udev_take_kernel_error(ctx->dev));
-    UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
+    if ((host_in || host_out) && prm->num_iterations > 0) {
+        /* the first and last iterations run eagerly, split where they meet
+         * host data (sirt_iteration_split), the others as graphs; a kernel
+         * error found afterwards still fails the call */
+        const unsigned int iters = prm->num_iterations;
+        UFOIR_TRY(sirt_iteration_split(&it, host_in, iters == 1 && host_out ? vol : NULL));
+        if (iters > 1) {
+            UFOIR_TRY(run_graphed(ctx, iters - 2, ufoir__sirt_body, &it));
+            UFOIR_TRY(sirt_iteration_split(&it, 0, host_out ? vol : NULL));
+        }
+        UFOIR_TRY(udev_copy_join(ctx->dev));
+        UFOIR_TRY(udev_take_kernel_error(ctx->dev));
+        UFOIR_TRY(ufoir__buf_out(ctx, &bx, 0));
+    } else {
+        UFOIR_TRY(run_graphed(ctx, prm->num_iterations, ufoir__sirt_body, &it));
+        UFOIR_TRY(udev_take_kernel_error(ctx->dev));
+        UFOIR_TRY(ufoir__buf_out(ctx, &bx, 1));
+    }
 done:
+    udev_copy_join(ctx->dev);     /* side copies finish before their buffers are freed */
     ufoir__free(ctx, R);
     ufoir__free(ctx, C);
     ufoir__fp_scratch_free(proj, &it.fs);

@@ -40,6 +40,22 @@ int udev_host_free(udev *d, void *p);
 int udev_is_device_ptr(udev *d, const void *p);
 int udev_memcpy_async(udev *d, void *dst, const void *src, size_t bytes);
 int udev_memcpy(udev *d, void *dst, const void *src, size_t bytes);   /* + stream sync */
+/* Copies on the context's side stream, overlapping the current stream's work:
+ * udev_copy_after starts a copy once everything enqueued on the current
+ * stream so far has run; udev_copy_join makes the current stream wait for
+ * every side copy issued so far. Not for use while the current stream is
+ * being captured. */
+int udev_copy_after(udev *d, void *dst, const void *src, size_t bytes);
+int udev_copy_join(udev *d);
+/* Finer control of the same side stream: udev_side_fence orders it after
+ * everything enqueued on the current stream so far; udev_side_copy issues a
+ * copy there with no new ordering and marks its end in event `slot`
+ * (0 <= slot < UDEV_SIDE_SLOTS); udev_side_wait makes the current stream wait
+ * for that mark. */
+#define UDEV_SIDE_SLOTS 8
+int udev_side_fence(udev *d);
+int udev_side_copy(udev *d, void *dst, const void *src, size_t bytes, int slot);
+int udev_side_wait(udev *d, int slot);
 
 /* ---- Device-side projection geometry (built by the host from the LUT). ---- */
 typedef struct {

@@ -30,6 +30,10 @@ struct udev {
     int *h_err = nullptr;
     int inject_skip_chunk = -1;     /* testing: see udev_inject_copy_skip */
     int sart_wide_clusters = 0;     /* 16-CTA clusters of the segment-form SART FP that fit at once */
+    cudaStream_t side = nullptr;    /* side copies (udev_copy_after), created on first use */
+    cudaEvent_t side_go = nullptr;  /* current stream -> side stream ordering */
+    cudaEvent_t side_done = nullptr;/* side stream -> current stream ordering */
+    cudaEvent_t side_mark[UDEV_SIDE_SLOTS] = {};  /* udev_side_copy marks */
 };
 
 /* One-time kernel attribute setup (dynamic shared memory opt-in). */

@@ -112,6 +112,17 @@ void udev_destroy(udev *d)
         cudaFree(d->d_err);
     if (d->h_err)
         cudaFreeHost(d->h_err);
+    if (d->side) {
+        cudaStreamSynchronize(d->side);
+        cudaStreamDestroy(d->side);
+    }
+    if (d->side_go)
+        cudaEventDestroy(d->side_go);
+    if (d->side_done)
+        cudaEventDestroy(d->side_done);
+    for (int i = 0; i < UDEV_SIDE_SLOTS; ++i)
+        if (d->side_mark[i])
+            cudaEventDestroy(d->side_mark[i]);
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
     delete d;
@@ -274,6 +285,77 @@ int udev_memcpy_async(udev *d, void *dst, const void *src, size_t bytes)
         return UFOIR_OK;
     UDEV_BIND(d);
     UDEV_CHECK(d, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, d->stream));
+    return UFOIR_OK;
+}
+
+static int side_ensure(udev *d)
+{
+    if (d->side)
+        return UFOIR_OK;
+    UDEV_CHECK(d, cudaStreamCreateWithFlags(&d->side, cudaStreamNonBlocking));
+    UDEV_CHECK(d, cudaEventCreateWithFlags(&d->side_go, cudaEventDisableTiming));
+    UDEV_CHECK(d, cudaEventCreateWithFlags(&d->side_done, cudaEventDisableTiming));
+    for (int i = 0; i < UDEV_SIDE_SLOTS; ++i)
+        UDEV_CHECK(d, cudaEventCreateWithFlags(&d->side_mark[i], cudaEventDisableTiming));
+    return UFOIR_OK;
+}
+
+int udev_side_fence(udev *d)
+{
+    UDEV_BIND(d);
+    int rc = side_ensure(d);
+    if (rc)
+        return rc;
+    UDEV_CHECK(d, cudaEventRecord(d->side_go, d->stream));
+    UDEV_CHECK(d, cudaStreamWaitEvent(d->side, d->side_go, 0));
+    return UFOIR_OK;
+}
+
+int udev_side_copy(udev *d, void *dst, const void *src, size_t bytes, int slot)
+{
+    if (slot < 0 || slot >= UDEV_SIDE_SLOTS) {
+        udev_set_error(d, "side copy: slot %d out of range", slot);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    int rc = side_ensure(d);
+    if (rc)
+        return rc;
+    if (bytes)
+        UDEV_CHECK(d, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, d->side));
+    UDEV_CHECK(d, cudaEventRecord(d->side_mark[slot], d->side));
+    return UFOIR_OK;
+}
+
+int udev_side_wait(udev *d, int slot)
+{
+    if (slot < 0 || slot >= UDEV_SIDE_SLOTS || !d->side) {
+        udev_set_error(d, "side wait: slot %d out of range or no side stream", slot);
+        return UFOIR_ERR_INVALID;
+    }
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaStreamWaitEvent(d->stream, d->side_mark[slot], 0));
+    return UFOIR_OK;
+}
+
+int udev_copy_after(udev *d, void *dst, const void *src, size_t bytes)
+{
+    if (bytes == 0)
+        return UFOIR_OK;
+    int rc = udev_side_fence(d);
+    if (rc)
+        return rc;
+    UDEV_CHECK(d, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, d->side));
+    return UFOIR_OK;
+}
+
+int udev_copy_join(udev *d)
+{
+    if (!d->side)
+        return UFOIR_OK;
+    UDEV_BIND(d);
+    UDEV_CHECK(d, cudaEventRecord(d->side_done, d->side));
+    UDEV_CHECK(d, cudaStreamWaitEvent(d->stream, d->side_done, 0));
     return UFOIR_OK;
 }
 
