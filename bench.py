@@ -246,6 +246,17 @@ def cpu_baseline(noisy_slice, gpu_result=None):
     return out
 
 
+def workload_config(S):
+    """The workload both arms measure (the reference arm on a bounded sample of it)."""
+    return {"workload": f"batched SIRT, {S} slices x {N_DETS}^2 grid ({PHANTOM}^2 phantoms), {N_ANGLES} angles, "
+                        f"{N_DETS} bins",
+            "slices_per_gpu": S, "n_dets": N_DETS, "n_angles": N_ANGLES, "relaxation_factor": RELAX}
+
+
+DATA = ("synthetic: seeded random-ellipse 1024^2 phantoms in a 1448^2 grid, Joseph FP, "
+        "Poisson noise I0=1e5, log")
+
+
 def run_reference(args, dist):
     """--impl reference: the reference's CPU path, rank 0 only."""
     if dist.rank != 0:
@@ -270,10 +281,11 @@ def run_reference(args, dist):
     return {"metric": METRIC, "value": value, "unit": "slice-iters/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"SIRT, {N_DETS}^2 grid (1024^2 ellipse phantom), {N_ANGLES} angles, "
-                                   f"{N_DETS} bins, one slice per step",
-                       "n_dets": N_DETS, "n_angles": N_ANGLES, "threads": threads},
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": {**workload_config(args.slices),
+                       "step": "a bounded sample of the workload: one SIRT iteration of one of its slices "
+                               "(all angles) per step, on the host cores",
+                       "threads": threads},
             "cpu_baseline": {"value": value, "unit": "slice-iters/s", "cores": threads, "kind": _cpu_kind(which),
                              "sample": sample},
             "e2e": {"value": value, "unit": "slice-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -377,11 +389,8 @@ def run_ufoir(args, dist):
     out = {"metric": METRIC, "value": value, "unit": "slice-iters/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic: seeded random-ellipse 1024^2 phantoms in a 1448^2 grid, Joseph FP, "
-                   "Poisson noise I0=1e5, log",
-           "config": {"workload": f"batched SIRT, {S} slices x 1448^2 grid (1024^2 phantoms), 1200 angles, "
-                                  "1448 bins",
-                      "slices_per_gpu": S, "n_dets": n, "n_angles": na, "relaxation_factor": RELAX,
+           "data": DATA,
+           "config": {**workload_config(S),
                       "step": "one SIRT iteration over all slices, one CUDA graph (pad+transpose, FP, BP)",
                       "l2": "inputs larger than L2 (about 3 GB resident working set per GPU)",
                       "parallelism": "replicas: slices sharded across ranks, no collective",
