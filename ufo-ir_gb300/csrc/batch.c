@@ -97,33 +97,51 @@ static int same_launch(const udev_fp_cfg *a, const udev_fp_cfg *b)
            a->fm == b->fm;
 }
 
+/* Releases the work lists, device tables and captured iteration of
+ * build_lists (so that they can be built again). */
+static void free_lists(ufoir_batch *b)
+{
+    ufoir_ctx *ctx = b->ctx;
+    udev_sync(ctx->dev);
+    udev_graph_destroy(b->exec);
+    b->exec = NULL;
+    b->exec_kernels = 0;
+    for (int k = 0; k < b->n_fp; k++) {
+        ufoir__free(ctx, b->fp[k].d_recs);
+        ufoir__free(ctx, b->fp[k].d_start);
+        ufoir__free(ctx, b->fp[k].d_jidx);
+    }
+    memset(b->fp, 0, sizeof(b->fp));
+    b->n_fp = 0;
+    ufoir__free(ctx, b->d_pad_recs);
+    ufoir__free(ctx, b->d_pad_start);
+    ufoir__free(ctx, b->d_ident);
+    b->d_pad_recs = NULL;
+    b->d_pad_start = b->d_ident = NULL;
+    for (int k = 0; k < 2; k++) {
+        ufoir__free(ctx, b->bp[k].d_recs);
+        ufoir__free(ctx, b->bp[k].d_start);
+        ufoir__free(ctx, b->bp[k].d_jidx);
+        b->bp[k].d_recs = NULL;
+        b->bp[k].d_start = b->bp[k].d_jidx = NULL;
+        b->bp[k].n_jobs = b->bp[k].items = 0;
+    }
+    ufoir__free(ctx, b->d_active);
+    b->d_active = NULL;
+}
+
 void ufoir_batch_destroy(ufoir_batch *b)
 {
     if (!b)
         return;
     ufoir_ctx *ctx = b->ctx;
     udev *d = ctx->dev;
-    udev_sync(d);
-    udev_graph_destroy(b->exec);
+    free_lists(b);
     for (int i = 0; i < b->n && b->owns; i++) {
         ufoir__free(ctx, b->m[i].resid);
         ufoir__free(ctx, b->m[i].P);
         ufoir__free(ctx, b->m[i].TP);
     }
-    for (int k = 0; k < b->n_fp; k++) {
-        ufoir__free(ctx, b->fp[k].d_recs);
-        ufoir__free(ctx, b->fp[k].d_start);
-        ufoir__free(ctx, b->fp[k].d_jidx);
-    }
-    ufoir__free(ctx, b->d_pad_recs);
-    ufoir__free(ctx, b->d_pad_start);
-    ufoir__free(ctx, b->d_ident);
-    for (int k = 0; k < 2; k++) {
-        ufoir__free(ctx, b->bp[k].d_recs);
-        ufoir__free(ctx, b->bp[k].d_start);
-        ufoir__free(ctx, b->bp[k].d_jidx);
-    }
-    ufoir__free(ctx, b->d_active);
     for (int i = 0; i < b->n_projs; i++) {
         ufoir__free(ctx, b->weights[2 * i]);
         ufoir__free(ctx, b->weights[2 * i + 1]);
@@ -436,6 +454,50 @@ static int shape_slices(ufoir_ctx *ctx, ufoir_projector **projs, const int *coun
     return rc;
 }
 
+/* Milliseconds of `iters` iterations of the batch as built, after one
+ * untimed one. The members' volumes are saved first and put back after, so
+ * the batch starts from them as if it had not run. */
+static int time_batch(ufoir_batch *b, unsigned int iters, float *ms)
+{
+    ufoir_ctx *ctx = b->ctx;
+    udev *d = ctx->dev;
+    size_t total = 0;
+    for (int i = 0; i < b->n; i++)
+        total += (size_t) b->m[i].p->n_dets * b->m[i].p->n_dets;
+    float *save = NULL;
+    int rc = ufoir__alloc(ctx, &save, total);
+    for (size_t i = 0, off = 0; (int) i < b->n && !rc; off += (size_t) b->m[i].p->n_dets * b->m[i].p->n_dets, i++)
+        rc = udev_memcpy_async(d, save + off, b->m[i].x, sizeof(float) * b->m[i].p->n_dets * b->m[i].p->n_dets);
+    if (!rc)
+        rc = ufoir__batch_launch(b, 1);
+    if (!rc)
+        rc = udev_timer_begin(d);
+    if (!rc)
+        rc = ufoir__batch_launch(b, iters);
+    if (!rc)
+        rc = udev_timer_end(d, ms);
+    for (size_t i = 0, off = 0; (int) i < b->n && !rc; off += (size_t) b->m[i].p->n_dets * b->m[i].p->n_dets, i++)
+        rc = udev_memcpy_async(d, b->m[i].x, save + off, sizeof(float) * b->m[i].p->n_dets * b->m[i].p->n_dets);
+    if (!rc)
+        rc = udev_sync(d);
+    if (!rc)
+        rc = udev_take_kernel_error(d);
+    ufoir__free(ctx, save);
+    return rc;
+}
+
+/* Launch shapes from the projectors' current state, then the lists. */
+static int shape_and_build(ufoir_batch *b, const int *geo_of, const int *geo_eff)
+{
+    free_lists(b);
+    for (int i = 0; i < b->n; i++) {
+        const int rc = member_shape(b->ctx, &b->m[i], geo_eff[geo_of[i]]);
+        if (rc)
+            return rc;
+    }
+    return build_lists(b);
+}
+
 int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_jobs, ufoir_batch **out)
 {
     if (!ctx || !jobs || !out || n_jobs == 0 || n_jobs > 65535)
@@ -510,16 +572,16 @@ int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_job
         geo_count[g]++;
     }
     UFOIR_TRY(shape_slices(ctx, b->projs, geo_count, b->n_projs, geo_eff));
-    /* With autotune on, each geometry's shape is searched; in a batch a
+    /* With autotune on, each geometry's shape is searched alone. In a batch a
      * tuned shape that differs from the fixed rules' adds a launch unless
-     * other members share it, and the search times each geometry alone, so
-     * a tuned shape is kept only where it wins by at least 10 %. */
+     * other members share it, so the batch with the tuned shapes is timed
+     * against the batch with the rules' shapes below and the faster kept. */
+    int any_tuned = 0;
     if (ctx->autotune)
         for (int g = 0; g < b->n_projs; g++) {
             ufoir_fp_tuning t;
             UFOIR_TRY(ufoir__fp_tune(b->projs[g], geo_eff[g], &t));
-            if (t.tuned && !(t.ms_tuned < 0.9f * t.ms_default))
-                b->projs[g]->fp_cfg_valid = 0;
+            any_tuned |= b->projs[g]->fp_cfg_valid;
         }
     for (int i = 0; i < n; i++) {
         const ufoir_batch_job *j = &jobs[i];
@@ -540,9 +602,57 @@ int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_job
         UFOIR_TRY(udev_memset(d, m->TP, 0, nn * pitch * sizeof(float)));
         if (!j->keep_vol)
             UFOIR_TRY(udev_fill(d, m->x, nn * nn, 0.0f));
-        UFOIR_TRY(member_shape(ctx, m, geo_eff[geo_of[i]]));
     }
-    UFOIR_TRY(build_lists(b));
+    UFOIR_TRY(shape_and_build(b, geo_of, geo_eff));
+    if (any_tuned) {
+        /* Where a tuned shape differs from the rules' one, the batch with the
+         * tuned shapes is timed against the batch with the rules' shapes, two
+         * iterations each on the members' own data (restored after), and the
+         * faster is kept. Every member's values are the same either way (the
+         * projections are invariant to the launch shape). */
+        int *valid = (int *) malloc(sizeof(int) * (size_t) b->n_projs);
+        udev_fp_cfg *tuned = (udev_fp_cfg *) malloc(sizeof(udev_fp_cfg) * (size_t) n);
+        if (!valid || !tuned) {
+            free(valid);
+            free(tuned);
+            rc = ufoir__fail(ctx, UFOIR_ERR_NOMEM, "out of host memory");
+            goto done;
+        }
+        for (int g = 0; g < b->n_projs; g++) {
+            valid[g] = b->projs[g]->fp_cfg_valid;
+            b->projs[g]->fp_cfg_valid = 0;
+        }
+        int differs = 0;
+        for (int i = 0; i < n && !rc; i++) {
+            tuned[i] = b->m[i].cfg;
+            rc = member_shape(ctx, &b->m[i], geo_eff[geo_of[i]]);     /* the rules' shape */
+            differs |= !same_launch(&tuned[i], &b->m[i].cfg);
+        }
+        float ms_tuned = 0.0f, ms_rules = 0.0f;
+        if (!rc && differs) {
+            rc = time_batch(b, 2, &ms_tuned);           /* the lists built so far are the tuned ones */
+            if (!rc) {
+                free_lists(b);
+                rc = build_lists(b);
+            }
+            if (!rc)
+                rc = time_batch(b, 2, &ms_rules);
+        }
+        for (int g = 0; g < b->n_projs; g++)
+            b->projs[g]->fp_cfg_valid = valid[g];
+        if (!rc && differs && ms_tuned < ms_rules)
+            rc = shape_and_build(b, geo_of, geo_eff);
+        else if (!rc && differs)
+            for (int g = 0; g < b->n_projs; g++)
+                b->projs[g]->fp_cfg_valid = 0;          /* the rules' shapes stay */
+        else
+            for (int i = 0; i < n; i++)
+                b->m[i].cfg = tuned[i];
+        free(valid);
+        free(tuned);
+        if (rc)
+            goto done;
+    }
     UFOIR_TRY(udev_sync(d));
     *out = b;
     b = NULL;
