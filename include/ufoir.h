@@ -388,7 +388,10 @@ typedef struct ufoir_batch ufoir_batch;
 
 /* Members need n_angles >= 16 and an axis at least half a pixel inside the
  * image (the tiled projectors; others give UFOIR_ERR_UNSUPPORTED). sino and
- * vol must stay valid until destroy. */
+ * vol must stay valid until destroy. With the context's autotune on, where a
+ * tuned shape differs from the fixed rules' one, creation times the batch
+ * both ways (one untimed and two timed iterations each, the members' volumes
+ * saved before and restored after) and keeps the faster. */
 UFOIR_API int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_jobs, ufoir_batch **out);
 /* Advances every active member by `iterations` SIRT iterations (synchronous). */
 UFOIR_API int ufoir_batch_run(ufoir_batch *b, unsigned int iterations);
