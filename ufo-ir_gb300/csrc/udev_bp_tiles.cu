@@ -7,7 +7,10 @@
  * per-angle set-up (16 pixels amortise it better than 8: 2.3 % on the C2
  * backprojection; 32 pixels, 32 x 256 tiles, need 139 KB of shared memory
  * and 132 registers, one CTA per SM, and were 23 % slower; a 64-register
- * build with 16-angle chunks, four CTAs per SM, was 6 % slower). For a chunk of
+ * build with 16-angle chunks, four CTAs per SM, was 6 % slower). Launches
+ * with fewer than three waves of such tiles (a single slice of 1448^2: 552
+ * tiles for 456 CTA slots) use 32 x 64 tiles, 8 pixels per thread, whose
+ * last wave is fuller. For a chunk of
  * 32 angles the CTA copies, per angle, the
  * 160 detector values that the tile can reach (cp.async, double buffered;
  * detectors outside [0, n) read 0), so every sample reads shared memory and
@@ -30,8 +33,8 @@ namespace {
 
 constexpr int kTX = 32;
 constexpr int kTY = 8;
-constexpr int kPY = 16;              /* pixels per thread (one column) */
-constexpr int kTileX = kTX;          /* tile is kTileX x kTileY pixels */
+constexpr int kPY = 16;              /* pixels per thread (one column); 8 for few-tile launches */
+constexpr int kTileX = kTX;          /* tile is kTileX x (kTY * PY) pixels */
 constexpr int kTileY = kTY * kPY;
 constexpr int kAC = 32;              /* angles per chunk */
 constexpr int kWin = 160;            /* detector window per angle (tile span <= 131, +5 margin, +3 alignment) */
@@ -64,13 +67,15 @@ struct BpTileArgs {
 
 /* Per angle of a chunk: cos, sin, and the first detector of its window
  * (as int bits); one 16-byte shared load. */
-struct __align__(16) BpSmem {
+template <int PY>
+struct __align__(16) BpSmemT {
     float win[2][kAC][kWin];
     float4 ang[2][kAC];
-    /* (-fY) * sin for the tile's 64 rows, [angle][ty][pixel p of the
-     * thread's column, 4 per float4]: the same for all 32 lanes of a warp */
-    float4 nys[2][kAC][kTY][kPY / 4];
+    /* (-fY) * sin for the tile's rows, [angle][ty][pixel p of the thread's
+     * column, 4 per float4]: the same for all 32 lanes of a warp */
+    float4 nys[2][kAC][kTY][PY / 4];
 };
+typedef BpSmemT<kPY> BpSmem;
 
 __device__ __forceinline__ void cp_async4(float *dst, const float *src)
 {
@@ -123,10 +128,11 @@ __device__ __forceinline__ float det_coord(float fX, float fY, float cs, float s
  * that cross the ends of the detector row go element by element, with zeros
  * outside [0, n).
  */
-template <bool FM>
-__device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, const float *sino, int x0, int y0,
+template <bool FM, int PY>
+__device__ void load_chunk(const BpTileArgs &P, BpSmemT<PY> &S, int buf, int chunk, const float *sino, int x0, int y0,
                            const joseph::AxisConsts &k, float e0, float e1, float shift)
 {
+    constexpr int kTileH = kTY * PY;
     const int tid = threadIdx.y * kTX + threadIdx.x;
     const int first = chunk * kAC;
     const int count = min(kAC, P.total_angles - first);
@@ -136,7 +142,7 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
         const float fx0 = __fsub_rn(__fadd_rn((float) x0, 0.5f), k.os);
         const float fx1 = __fsub_rn(__fadd_rn((float) (x0 + kTileX - 1), 0.5f), k.os);
         const float fy0 = __fsub_rn(__fadd_rn((float) y0, 0.5f), k.os);
-        const float fy1 = __fsub_rn(__fadd_rn((float) (y0 + kTileY - 1), 0.5f), k.os);
+        const float fy1 = __fsub_rn(__fadd_rn((float) (y0 + kTileH - 1), 0.5f), k.os);
         const float c00 = det_coord(fx0, fy0, cs, sn, shift), c10 = det_coord(fx1, fy0, cs, sn, shift);
         const float c01 = det_coord(fx0, fy1, cs, sn, shift), c11 = det_coord(fx1, fy1, cs, sn, shift);
         float lo = fminf(fminf(c00, c10), fminf(c01, c11));
@@ -150,11 +156,11 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
     /* row products of the chunk's angles, rounded as the in-loop product
      * (fast arithmetic: with the shift already added) */
     float *nys = reinterpret_cast<float *>(&S.nys[buf][0][0][0]);
-    for (int idx = tid; idx < count * kTileY; idx += kTX * kTY) {
-        const int slot = idx / kTileY, r = idx % kTileY;      /* row r = ty + kTY * p */
+    for (int idx = tid; idx < count * kTileH; idx += kTX * kTY) {
+        const int slot = idx / kTileH, r = idx % kTileH;      /* row r = ty + kTY * p */
         const float nfy = -__fsub_rn(__fadd_rn((float) (y0 + r), 0.5f), k.os);
         const float prod = __fmul_rn(nfy, S.ang[buf][slot].y);
-        nys[(slot * kTY + r % kTY) * kPY + r / kTY] = FM ? __fadd_rn(prod, shift) : prod;
+        nys[(slot * kTY + r % kTY) * PY + r / kTY] = FM ? __fadd_rn(prod, shift) : prod;
     }
     constexpr int kGroups = kWin / 4;
     for (int idx = tid; idx < count * kGroups; idx += kTX * kTY) {
@@ -182,10 +188,10 @@ __device__ void load_chunk(const BpTileArgs &P, BpSmem &S, int buf, int chunk, c
  * packed instruction. FAST: every clamped coordinate is >= 0.5, so the
  * three-step floor applies.
  */
-template <bool CLAMP, bool FAST, bool FM>
-__device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count, int first_vi, const BpTileArgs &P,
-                                             float fX, float shift, float e0, float e1,
-                                             float2 sum[kPY / 2], float2 v[kPY / 2], int &sub, int &sub_end)
+template <bool CLAMP, bool FAST, bool FM, int PY>
+__device__ __forceinline__ void sample_chunk(const BpSmemT<PY> &S, int buf, int count, int first_vi,
+                                             const BpTileArgs &P, float fX, float shift, float e0, float e1,
+                                             float2 sum[PY / 2], float2 v[PY / 2], int &sub, int &sub_end)
 {
     const uint32_t win0 = (uint32_t) __cvta_generic_to_shared(&S.win[buf][0][0]);
     const uint32_t bits = FAST ? (uint32_t) joseph::kHalfFloorBits : (uint32_t) joseph::kFloorMagicBits;
@@ -196,7 +202,7 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
         if (vi == sub_end) {
             /* end of a subset: v = v + relax * sum (one BP launch of the reference) */
 #pragma unroll
-            for (int q = 0; q < kPY / 2; ++q) {
+            for (int q = 0; q < PY / 2; ++q) {
                 v[q] = joseph::add2(v[q], joseph::mul2z(joseph::splat(P.relax), sum[q], joseph::splat(P.neg_zero)));
                 sum[q] = make_float2(0.0f, 0.0f);
             }
@@ -204,9 +210,9 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
             sub_end += (int) P.sub_n[sub];
         }
         const float4 ang = S.ang[buf][i];
-        float2 nys[kPY / 2];
+        float2 nys[PY / 2];
 #pragma unroll
-        for (int f = 0; f < kPY / 4; ++f) {
+        for (int f = 0; f < PY / 4; ++f) {
             const float4 ny = S.nys[buf][i][threadIdx.y][f];
             nys[2 * f] = make_float2(ny.x, ny.y);
             nys[2 * f + 1] = make_float2(ny.z, ny.w);
@@ -215,7 +221,7 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
         const uint32_t base = win0 + 4u * (uint32_t) (i * kWin) - 4u * ((uint32_t) __float_as_int(ang.z) + bits);
         const float2 fxc = joseph::splat(__fmul_rn(fX, ang.x));
 #pragma unroll
-        for (int q = 0; q < kPY / 2; ++q) {
+        for (int q = 0; q < PY / 2; ++q) {
             /* fX * cos - fY * sin + shift, as fX*cos + (-fY)*sin + shift
              * (fast arithmetic: fX*cos + ((-fY)*sin + shift)) */
             float2 sc = FM ? joseph::add2(fxc, nys[q]) : joseph::add2(joseph::add2(fxc, nys[q]), shift2);
@@ -235,13 +241,14 @@ __device__ __forceinline__ void sample_chunk(const BpSmem &S, int buf, int count
 }
 
 /* One CTA's work: pixel tile `tile` of slice `slice`. */
-template <bool FM>
-__device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile, int slice)
+template <bool FM, int PY>
+__device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmemT<PY> &S, int tile, int slice)
 {
+    constexpr int kTileH = kTY * PY;
     const int n = P.n;
     const int tiles_x = (n + kTileX - 1) / kTileX;
     const int x0 = (tile % tiles_x) * kTileX;
-    const int y0 = (tile / tiles_x) * kTileY;
+    const int y0 = (tile / tiles_x) * kTileH;
     const float *sino = P.sino + (size_t) slice * P.sino_stride;
 
     const joseph::AxisConsts k = joseph::axis_consts(n, P.axis);
@@ -252,9 +259,9 @@ __device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile
     const int x = x0 + (int) threadIdx.x;
     const float fX = __fsub_rn(__fadd_rn((float) x, 0.5f), k.os);
     /* pixel pairs (p, p + 1) of the thread's column */
-    float2 sum[kPY / 2], v[kPY / 2];
+    float2 sum[PY / 2], v[PY / 2];
 #pragma unroll
-    for (int q = 0; q < kPY / 2; ++q) {
+    for (int q = 0; q < PY / 2; ++q) {
         float b[2];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -274,7 +281,7 @@ __device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile
     if (k.diff == 0.0f) {
         const float r = 0.5f * (float) n - 2.0f;
         const float ax = fmaxf(fabsf((float) x0 - k.os), fabsf((float) (x0 + kTileX) - k.os));
-        const float ay = fmaxf(fabsf((float) y0 - k.os), fabsf((float) (y0 + kTileY) - k.os));
+        const float ay = fmaxf(fabsf((float) y0 - k.os), fabsf((float) (y0 + kTileH) - k.os));
         clamp = ax * ax + ay * ay > r * r;
     }
     /* clamped coordinates are >= min(e0, e1) */
@@ -284,13 +291,13 @@ __device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile
     int sub = 0;
     int sub_end = P.n_subsets > 0 ? (int) P.sub_n[0] : 0;
     if (nchunks > 0) {
-        load_chunk<FM>(P, S, 0, 0, sino, x0, y0, k, e0, e1, shift);
+        load_chunk<FM, PY>(P, S, 0, 0, sino, x0, y0, k, e0, e1, shift);
         cp_async_commit();
     }
     for (int ch = 0; ch < nchunks; ++ch) {
         const int buf = ch & 1;
         if (ch + 1 < nchunks) {
-            load_chunk<FM>(P, S, buf ^ 1, ch + 1, sino, x0, y0, k, e0, e1, shift);
+            load_chunk<FM, PY>(P, S, buf ^ 1, ch + 1, sino, x0, y0, k, e0, e1, shift);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -299,22 +306,22 @@ __device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile
         __syncthreads();
         const int count = min(kAC, P.total_angles - ch * kAC);
         if (!clamp)
-            sample_chunk<false, true, FM>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<false, true, FM, PY>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         else if (fast)
-            sample_chunk<true, true, FM>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, true, FM, PY>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         else
-            sample_chunk<true, false, FM>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
+            sample_chunk<true, false, FM, PY>(S, buf, count, ch * kAC, P, fX, shift, e0, e1, sum, v, sub, sub_end);
         __syncthreads();
     }
     if (P.n_subsets > 0) {
 #pragma unroll
-        for (int q = 0; q < kPY / 2; ++q)
+        for (int q = 0; q < PY / 2; ++q)
             v[q] = joseph::add2(v[q], joseph::mul2z(joseph::splat(P.relax), sum[q], joseph::splat(P.neg_zero)));
     }
     if (x >= n)
         return;
 #pragma unroll
-    for (int p = 0; p < kPY; ++p) {
+    for (int p = 0; p < PY; ++p) {
         const int y = y0 + (int) threadIdx.y + kTY * p;
         if (y >= n)
             continue;
@@ -328,11 +335,11 @@ __device__ __forceinline__ void bp_tile(const BpTileArgs &P, BpSmem &S, int tile
     }
 }
 
-template <bool FM>
+template <bool FM, int PY>
 __global__ void __launch_bounds__(kTX * kTY) bp_tiles_kernel(const __grid_constant__ BpTileArgs P)
 {
-    __shared__ BpSmem S;
-    bp_tile<FM>(P, S, (int) blockIdx.x, (int) blockIdx.y);
+    __shared__ BpSmemT<PY> S;
+    bp_tile<FM, PY>(P, S, (int) blockIdx.x, (int) blockIdx.y);
 }
 
 /*
@@ -374,7 +381,7 @@ __global__ void __launch_bounds__(kTX * kTY, 3) bp_tiles_batch_kernel(const BpTi
             dst[e] = __ldg(src + e);
     }
     __syncthreads();
-    bp_tile<FM>(rec, S, b - __ldg(item_start + j), 0);
+    bp_tile<FM, kPY>(rec, S, b - __ldg(item_start + j), 0);
 }
 
 static_assert(sizeof(BpTileArgs) % sizeof(int) == 0, "records are copied as ints");
@@ -474,9 +481,16 @@ extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *su
     if (rc0)
         return rc0;
     UDEV_BIND(d);
+    /* Tiles of 16 pixels per thread (32 x 128) unless the launch has fewer than
+     * three waves of them (three CTAs per SM): then 8 per thread (32 x 64), whose
+     * last wave is fuller. At 1448^2 x 1200 one slice's BP took 1.131 instead of
+     * 1.194 ms, two slices' 2.155 instead of 2.266; three slices (3.6 waves)
+     * keep the tall tiles (3.130 against 3.197 ms). */
     const int tiles_x = (g->n_dets + kTileX - 1) / kTileX;
-    const int tiles_y = (g->n_dets + kTileY - 1) / kTileY;
-    const unsigned int n_tiles = (unsigned int) (tiles_x * tiles_y);
+    const long long tiles16 = (long long) tiles_x * ((g->n_dets + kTileY - 1) / kTileY);
+    const bool short_tiles = tiles16 * n_slices < 3LL * 3 * udev_sm_count(d);
+    const int tile_h = short_tiles ? kTY * 8 : kTileY;
+    const unsigned int n_tiles = (unsigned int) (tiles_x * ((g->n_dets + tile_h - 1) / tile_h));
     for (int done = 0; done < n_slices;) {
         const int chunk = n_slices - done > 65535 ? 65535 : n_slices - done;
         BpTileArgs B = A;
@@ -488,10 +502,15 @@ extern "C" int udev_bp_tiles(udev *d, const udev_geom *g, const ufoir_subset *su
         if (B.add)
             B.add += (size_t) done * A.vol_stride;
         B.dst += (size_t) done * A.vol_stride;
-        if (g->fast_arith)
-            bp_tiles_kernel<true><<<dim3(n_tiles, (unsigned int) chunk), dim3(kTX, kTY), 0, d->stream>>>(B);
+        const dim3 grid(n_tiles, (unsigned int) chunk), block(kTX, kTY);
+        if (g->fast_arith && short_tiles)
+            bp_tiles_kernel<true, 8><<<grid, block, 0, d->stream>>>(B);
+        else if (g->fast_arith)
+            bp_tiles_kernel<true, kPY><<<grid, block, 0, d->stream>>>(B);
+        else if (short_tiles)
+            bp_tiles_kernel<false, 8><<<grid, block, 0, d->stream>>>(B);
         else
-            bp_tiles_kernel<false><<<dim3(n_tiles, (unsigned int) chunk), dim3(kTX, kTY), 0, d->stream>>>(B);
+            bp_tiles_kernel<false, kPY><<<grid, block, 0, d->stream>>>(B);
         int rc = udev_after_launch(d, "bp_tiles_kernel");
         if (rc)
             return rc;
