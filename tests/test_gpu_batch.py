@@ -54,7 +54,7 @@ def test_mixed_batch_equals_each_job_alone(ufoir_lib, gpu_ctx, autotune):
             b.run(2)
             got5 = [v.download() for v in d_v]
     finally:
-        gpu_ctx.set_autotune(False)
+        gpu_ctx.set_autotune(ufoir.AUTOTUNE_AUTO)      # the context default
     for k, (s, st, ax, rl) in enumerate(mem):
         want3 = _alone(ufoir, gpu_ctx, s, st, ax, rl, 3)
         assert np.array_equal(got3[k], want3), (k, MIX[k], float(np.abs(got3[k] - want3).max()))
@@ -129,3 +129,30 @@ def test_autotuned_forward_projection_is_unchanged(ufoir_lib, gpu_ctx, oracle, n
     assert np.array_equal(after[0], oracle.forward(oracle.projector(n, na, step), vols[0]))
     print(f"\nautotune {n}^2 x {na}, {slices} slices: {t}")
     p.close()
+
+
+# The default mode (AUTO) searches launch shapes for SIRT calls whose tiles
+# cannot fill the GPU (one slice: the fixed rules split detectors there).
+# Whatever it picks, the result equals the fixed rules' bit for bit.
+@pytest.mark.parametrize("n,na", [(724, 64), (1448, 40), (300, 97)])
+def test_auto_search_keeps_results(ufoir_lib, gpu_ctx, n, na):
+    ufoir = ufoir_lib
+    step = np.float32(np.pi / na)
+    sino = np.random.default_rng(n + na).random((na, n), dtype=np.float32) * n
+    out = {}
+    for mode in (ufoir.AUTOTUNE_OFF, ufoir.AUTOTUNE_AUTO):
+        gpu_ctx.set_autotune(mode)
+        try:
+            p = ufoir.ParallelProjector(gpu_ctx, step=float(step), is_forward=0)
+            out[mode] = ufoir.sirt(p, sino, num_iterations=3, relaxation_factor=0.25)
+            p.close()
+        finally:
+            gpu_ctx.set_autotune(ufoir.AUTOTUNE_AUTO)
+    assert np.array_equal(out[ufoir.AUTOTUNE_OFF], out[ufoir.AUTOTUNE_AUTO])
+
+
+def test_autotune_mode_argument_checks(ufoir_lib, gpu_ctx):
+    L = ufoir_lib.lib()
+    assert L.ufoir_ctx_set_autotune(gpu_ctx.handle, 3) == ufoir_lib.ERR_INVALID
+    assert L.ufoir_ctx_set_autotune(gpu_ctx.handle, -1) == ufoir_lib.ERR_INVALID
+    assert L.ufoir_ctx_set_autotune(gpu_ctx.handle, ufoir_lib.AUTOTUNE_AUTO) == ufoir_lib.OK

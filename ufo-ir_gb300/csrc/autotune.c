@@ -27,6 +27,7 @@
 struct ufoir__tune_entry {
     unsigned int n, na;
     float step, axis;
+    int arithmetic;          /* the shape carries the kernel's arithmetic (cfg.fm) */
     int slices;
     udev_fp_cfg cfg;
     ufoir_fp_tuning info;
@@ -45,7 +46,7 @@ static struct ufoir__tune_entry *tune_find(ufoir_ctx *ctx, const ufoir_projector
     for (int i = 0; i < ctx->n_tune; i++) {
         struct ufoir__tune_entry *e = &ctx->tune[i];
         if (e->n == p->n_dets && e->na == p->n_angles && e->step == p->lut_step && e->axis == axis &&
-            e->slices == slices)
+            e->arithmetic == p->prm.arithmetic && e->slices == slices)
             return e;
     }
     return NULL;
@@ -220,6 +221,7 @@ int ufoir__fp_tune(ufoir_projector *p, int n_slices, ufoir_fp_tuning *out)
         e->na = p->n_angles;
         e->step = p->lut_step;
         e->axis = ufoir__axis(p);
+        e->arithmetic = p->prm.arithmetic;
         e->slices = n_slices;
         e->cfg = best;
         e->info = info;
@@ -236,6 +238,24 @@ done:
     ufoir__free(ctx, sino);
     udev_sync(d);
     return rc;
+}
+
+int ufoir__fp_tune_wanted(ufoir_projector *p, int n_slices)
+{
+    const int mode = p->ctx->autotune;
+    if (mode == UFOIR_AUTOTUNE_ON)
+        return 1;
+    if (mode != UFOIR_AUTOTUNE_AUTO || !p->have_geometry || n_slices < 1)
+        return 0;
+    /* the fixed rules' shape for this call (a shape already tuned for it is set aside) */
+    const int valid = p->fp_cfg_valid;
+    p->fp_cfg_valid = 0;
+    udev_fp_cfg c;
+    const void *tiles = NULL;
+    int n_tiles = 0;
+    const int rc = ufoir__fp_shape(p, n_slices, &c, &tiles, &n_tiles);
+    p->fp_cfg_valid = valid;
+    return rc == UFOIR_OK && c.dsplit > 1;
 }
 
 int ufoir_projector_autotune(ufoir_projector *proj, size_t n_slices, ufoir_fp_tuning *out)

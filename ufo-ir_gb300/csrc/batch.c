@@ -577,7 +577,7 @@ int ufoir_batch_create(ufoir_ctx *ctx, const ufoir_batch_job *jobs, size_t n_job
      * other members share it, so the batch with the tuned shapes is timed
      * against the batch with the rules' shapes below and the faster kept. */
     int any_tuned = 0;
-    if (ctx->autotune)
+    if (ctx->autotune == UFOIR_AUTOTUNE_ON)
         for (int g = 0; g < b->n_projs; g++) {
             ufoir_fp_tuning t;
             UFOIR_TRY(ufoir__fp_tune(b->projs[g], geo_eff[g], &t));

@@ -37,6 +37,7 @@ int ufoir_ctx_create(int device, uint64_t hbm_budget_bytes, ufoir_ctx **out)
         free(ctx);
         return rc;
     }
+    ctx->autotune = UFOIR_AUTOTUNE_AUTO;
     if (hbm_budget_bytes == 0) {
         size_t fr = 0, tot = 0;
         if (udev_mem_info(ctx->dev, &fr, &tot) == UFOIR_OK)
@@ -63,7 +64,7 @@ int ufoir_ctx_sm_count(const ufoir_ctx *ctx)
 
 int ufoir_ctx_set_autotune(ufoir_ctx *ctx, int on)
 {
-    if (!ctx || (on != 0 && on != 1))
+    if (!ctx || (on != UFOIR_AUTOTUNE_OFF && on != UFOIR_AUTOTUNE_ON && on != UFOIR_AUTOTUNE_AUTO))
         return UFOIR_ERR_INVALID;
     ctx->autotune = on;
     return UFOIR_OK;

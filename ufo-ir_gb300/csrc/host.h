@@ -16,7 +16,7 @@ struct ufoir_ctx {
     udev *dev;
     uint64_t hbm_budget;
     char create_err[256];
-    int autotune;                       /* 1: forward-projector launch shapes are searched per geometry */
+    int autotune;                       /* UFOIR_AUTOTUNE_*: forward-projector launch-shape search */
     struct ufoir__tune_entry *tune;     /* cache of searched shapes (autotune.c) */
     int n_tune, cap_tune;
 };
@@ -134,11 +134,15 @@ int ufoir__projector_tiles(ufoir_projector *p, int A, const void **d_tiles, int 
  * (its tiles are built then), else the fixed rules. UFOIR_ERR_UNSUPPORTED if
  * the tiled kernel cannot serve the size. */
 int ufoir__fp_shape(ufoir_projector *p, int n_slices, udev_fp_cfg *c, const void **d_tiles, int *n_tiles);
-/* Autotuner (autotune.c): with the context's autotune on, searches the
- * launch shapes for this geometry and n_slices (once per context; cached)
- * and records the fastest on the projector. A no-op when autotune is off.
- * Must not run inside a stream capture. */
+/* Autotuner (autotune.c): searches the launch shapes for this geometry and
+ * n_slices (once per context; cached) and records the fastest on the
+ * projector. Must not run inside a stream capture. */
 int ufoir__fp_tune(ufoir_projector *p, int n_slices, ufoir_fp_tuning *out);
+/* Whether a SIRT call on n_slices slices should search first: always with
+ * UFOIR_AUTOTUNE_ON, with UFOIR_AUTOTUNE_AUTO where the fixed rules would
+ * split each angle tile's detectors over several CTAs (too few tiles to fill
+ * the GPU, where the rules were measured 11-32 % off the best shape). */
+int ufoir__fp_tune_wanted(ufoir_projector *p, int n_slices);
 void ufoir__tune_free(ufoir_ctx *ctx);
 
 /* A member of a mixed SIRT batch whose buffers its owner keeps (the serve

@@ -284,7 +284,7 @@ int ufoir_sirt_process(ufoir_projector *proj, const ufoir_sirt_params *prm, cons
     proj->prm.relaxation = prm->relaxation_factor;
     proj->prm.correction_scale = -1.0f;
     UFOIR_TRY(udev_fill(ctx->dev, bx.dev, nv * n_slices, 0.0f));
-    if (ctx->autotune)
+    if (ufoir__fp_tune_wanted(proj, (int) n_slices))
         UFOIR_TRY(ufoir__fp_tune(proj, (int) n_slices, NULL));
 
     it.p = proj;
@@ -388,7 +388,7 @@ int ufoir_sirt_batch_create(ufoir_projector *proj, const ufoir_sirt_params *prm,
     proj->prm.relaxation = prm->relaxation_factor;
     proj->prm.correction_scale = -1.0f;
     UFOIR_TRY(udev_fill(ctx->dev, d_vol, nv * n_slices, 0.0f));
-    if (ctx->autotune)
+    if (ufoir__fp_tune_wanted(proj, (int) n_slices))
         UFOIR_TRY(ufoir__fp_tune(proj, (int) n_slices, NULL));
     b->it.p = proj;
     ufoir__projector_geom(proj, &b->it.g);

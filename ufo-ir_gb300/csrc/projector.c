@@ -381,7 +381,8 @@ int ufoir__fp_shape(ufoir_projector *p, int n_slices, udev_fp_cfg *c, const void
     udev *d = p->ctx->dev;
     udev_geom g;
     ufoir__projector_geom(p, &g);
-    if (p->fp_cfg_valid && p->fp_cfg_slices == n_slices) {
+    /* a tuned shape serves only the slice count and arithmetic it was timed for */
+    if (p->fp_cfg_valid && p->fp_cfg_slices == n_slices && p->fp_cfg.fm == (g.fast_arith ? 1 : 0)) {
         *c = p->fp_cfg;
         return ufoir__projector_tiles(p, c->A, d_tiles, n_tiles, NULL);
     }

@@ -729,6 +729,9 @@ int ufoir_serve_create(ufoir_ctx *ctx, const ufoir_serve_config *cfg, ufoir_serv
         s->cfg.max_active_jobs = 1024;
     s->user_ctx = ctx;
     int rc = ufoir_ctx_create(udev_device(ctx->dev), s->cfg.hbm_budget_bytes, &s->ctx);
+    /* jobs rarely share a geometry: no launch-shape search inside a job's latency */
+    if (rc == UFOIR_OK)
+        rc = ufoir_ctx_set_autotune(s->ctx, UFOIR_AUTOTUNE_OFF);
     if (rc) {
         free(s);
         return ufoir__fail(ctx, rc, "serve: private context: %s", ufoir_last_error(NULL));

@@ -38,6 +38,7 @@ NORM_COMPAT = 0
 NORM_FP64 = 1
 ARITH_EXACT = 0
 ARITH_FAST = 1
+AUTOTUNE_OFF, AUTOTUNE_ON, AUTOTUNE_AUTO = 0, 1, 2
 
 
 class UfoirError(RuntimeError):
@@ -409,8 +410,10 @@ class Context:
     def sm_count(self) -> int:
         return int(lib().ufoir_ctx_sm_count(self.handle))
 
-    def set_autotune(self, on: bool):
-        self._check(lib().ufoir_ctx_set_autotune(self.handle, int(bool(on))))
+    def set_autotune(self, on):
+        """False/True (off/on) or AUTOTUNE_AUTO (the default)."""
+        mode = on if isinstance(on, int) and not isinstance(on, bool) else int(bool(on))
+        self._check(lib().ufoir_ctx_set_autotune(self.handle, mode))
 
     def l1_norm(self, v, mode=NORM_FP64) -> float:
         out = C.c_float()
