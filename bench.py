@@ -194,7 +194,7 @@ def make_inputs(ufoir, ctx, proj, rank, S):
 
 def _cpu_oracle():
     """The oracle (test infrastructure, used here only as the CPU baseline and
-    the checker) with all host threads; which = "ref" when the reference's
+    as the reference result to compare with) with all host threads; which = "ref" when the reference's
     own kernels were built (oracle/_ref), else "port"."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
@@ -217,7 +217,7 @@ def _cpu_what(which):
 def cpu_baseline(noisy_slice, gpu_result=None):
     """The reference's CPU path on one slice of the workload: one full SIRT
     iteration (all 1200 angles). With gpu_result (slice 0 of the e2e call,
-    E2E_ITERS iterations), also the checker: the oracle's result and its FP64
+    E2E_ITERS iterations), also the accuracy check: the oracle's result and its FP64
     twin's for the same call, and their relative L2 errors."""
     pyoracle, threads, which = _cpu_oracle()
     step = np.float32(np.pi / N_ANGLES)
@@ -236,7 +236,7 @@ def cpu_baseline(noisy_slice, gpu_result=None):
         want_d = pyoracle.sirt_d(pyoracle.projector(N_DETS, N_ANGLES, step), sino, E2E_ITERS, RELAX)
         g = np.asarray(gpu_result, np.float64)
         out["accuracy"] = {
-            "result": f"slice 0 of the e2e call ({E2E_ITERS} SIRT iterations)", "checker": _cpu_what(which),
+            "result": f"slice 0 of the e2e call ({E2E_ITERS} SIRT iterations)", "compared_with": _cpu_what(which),
             "rel_l2_vs_oracle": float(np.linalg.norm(g - want) / np.linalg.norm(want)),
             "bit_exact_vs_oracle": bool(np.array_equal(gpu_result, want)),
             "rel_l2_vs_fp64_twin": float(np.linalg.norm(g - want_d) / np.linalg.norm(want_d)),

@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the product library links or calls this
  * code; it is loaded by the tests, by __graft_entry__.smoke() and by the CPU
- * baseline leg of bench.py, always as the checker, never as the thing measured.
+ * baseline leg of bench.py, always as the result compared with, never as the
+ * thing measured.
  *
  * Contents:
  *   - a plain-C restatement of the reference's OpenCL kernels

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/liboracle.so, oracle/_ref/libufoir_ref.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and
-by the CPU-baseline leg of ``bench.py``, always as the checker. The product
+by the CPU-baseline leg of ``bench.py``, always as the result compared with. The product
 (``ufo-ir_gb300``) never imports this module.
 
 Arrays are numpy, C-contiguous: sinograms ``[n_angles, n_dets]``, volumes

@@ -1,7 +1,7 @@
 """The projector's fast interpolation arithmetic ("arithmetic": "fast"), an
 extension with no counterpart in the reference, through the C ABI.
 
-Tolerance (the benchmark spec's for this path): relative L2 <= 1e-5 against the
+Tolerance (the path's stated bar): relative L2 <= 1e-5 against the
 reference arithmetic after one projection, <= 1e-4 after the stated
 iteration count (100 SIRT iterations at the 1448^2 x 1200-angle geometry).
 The exact arithmetic is checked bit for bit against the oracle elsewhere;

@@ -1,6 +1,6 @@
 """GPU parity of SART, SIRT, ASD-POCS and split-Bregman TV through the C ABI.
 
-Tolerance (the benchmark spec): relative L2 error <= 1e-4 after the stated number of
+Tolerance (the path's stated bar): relative L2 error <= 1e-4 after the stated number of
 iterations. In COMPAT norm mode every operation, including the host-side
 float sums, is the reference's, so results are also required to be equal
 bit for bit to the oracle and to the golden fixtures.

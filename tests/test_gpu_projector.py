@@ -1,6 +1,6 @@
 """GPU parity of the projector (FP / BP / process / subsets) through the C ABI.
 
-Tolerance (the benchmark spec): relative L2 error <= 1e-5 after one application.
+Tolerance (the path's stated bar): relative L2 error <= 1e-5 after one application.
 The kernels follow the reference's operation order exactly, so the tests
 also require bit equality with the oracle and the golden fixtures (made by
 the reference's own kernel sources) wherever the inputs are identical.

@@ -2,15 +2,18 @@
  * serve.c - continuous-batching request loop for reconstruction jobs.
  *
  * One worker thread owns a private context (its own streams) on the caller's
- * GPU. Jobs wait in arrival order; the worker admits the head of the queue
- * whenever the active-job limit and the HBM budget allow, sets the job up on
- * its own CUDA stream (sinogram upload, weights, one captured CUDA graph per
- * iteration or sweep), and then advances all active jobs round-robin, one
- * quantum per turn, issuing a job's next quantum only when its previous one
- * has finished (an event query, never a blocking wait). Different jobs'
- * kernels therefore run side by side on the GPU and a queued job starts as
- * soon as memory frees up. Each job runs exactly the kernels of the plain
- * ufoir_*_process call on one slice, so its result is independent of the mix.
+ * GPU. Jobs wait in arrival order; the worker admits queued jobs whenever the
+ * active-job limit and the HBM budget allow (which job, per policy:
+ * pick_admission), sets each up on its own CUDA stream (sinogram upload,
+ * weights, one captured CUDA graph per iteration or sweep), and then gives
+ * quanta to the idle active jobs with the least remaining work first, at
+ * most max_running with work in flight, issuing a job's next quantum only
+ * when its previous one has finished (an event query, never a blocking
+ * wait). Different jobs' kernels therefore run side by side on the GPU and a
+ * queued job starts as soon as memory frees up. Each job runs exactly the
+ * kernels of the plain ufoir_*_process call on one slice (or, with
+ * batch_sirt, of a mixed batch, whose members equal their runs alone), so
+ * its result is independent of the mix.
  */
 #include <errno.h>
 #include <pthread.h>
