@@ -708,13 +708,26 @@ __global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
     float *vcol = P.vol + (size_t) blockIdx.z * P.vol_stride + (size_t) (j_base + (int) threadIdx.y) * P.pitch +
                   kSartPadL + i0;
     const int rows_left = n - j_base - (int) threadIdx.y;     /* rows m with 8m < rows_left exist */
+    /* a tile wholly inside the image (uniform per CTA) loads and stores
+     * every pixel without the per-pixel checks */
+    const bool full = i_base + kBpTileW <= n && j_base + 8 * ROWS <= n;
     float x[ROWS][4];
+    if (full) {
 #pragma unroll
-    for (int m = 0; m < ROWS; ++m) {
-        const float *row = vcol + (size_t) (8 * m) * P.pitch;
+        for (int m = 0; m < ROWS; ++m) {
+            const float *row = vcol + (size_t) (8 * m) * P.pitch;
 #pragma unroll
-        for (int h = 0; h < 4; ++h)
-            x[m][h] = okc[h] && 8 * m < rows_left ? row[32 * h] : 0.0f;
+            for (int h = 0; h < 4; ++h)
+                x[m][h] = row[32 * h];
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < ROWS; ++m) {
+            const float *row = vcol + (size_t) (8 * m) * P.pitch;
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                x[m][h] = okc[h] && 8 * m < rows_left ? row[32 * h] : 0.0f;
+        }
     }
     const float *r = P.sino + (size_t) blockIdx.z * P.sino_stride + (size_t) P.angle * n;
     for (int k = tid; k < span; k += 256) {
@@ -743,6 +756,16 @@ __global__ void __launch_bounds__(256) sart_bp_kernel(SartBpArgs P)
         sart_bp_rows<T, ROWS, false>(P, x, pc, j0, rbase, relax, z2);
     else
         sart_bp_rows<T, ROWS, true>(P, x, pc, j0, rbase, relax, z2);
+    if (full) {
+#pragma unroll
+        for (int m = 0; m < ROWS; ++m) {
+            float *row = vcol + (size_t) (8 * m) * P.pitch;
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                row[32 * h] = x[m][h];
+        }
+        return;
+    }
 #pragma unroll
     for (int m = 0; m < ROWS; ++m) {
         if (8 * m < rows_left) {
